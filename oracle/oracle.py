@@ -1,0 +1,395 @@
+"""Python driver for the CPU oracle (test infrastructure only).
+
+Wraps ``liborc.so`` (oracle/de_oracle.c) with ctypes and runs the reference's
+time-stepping loop around it.  Used by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of bench.py as the parity checker; never by the product.
+
+The loop mirrors the reference:
+
+* ``_evolve_base``            abstract_2d_finite_volumes/generic_domain.py:1715-1912
+* ``evolve_one_euler_step``   generic_domain.py:1914-1972
+* ``evolve_one_rk2_step``     generic_domain.py:1974-2051
+* ``update_timestep``         generic_domain.py:2349-2415
+* ``update_conserved_quantities`` shallow_water/shallow_water_domain.py:2089-2163
+* ``Rate_operator.__call__``  operators/rate_operators.py:149-258 (constant rates)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liborc.so")
+
+EPSILON = 1.0e-12   # anuga/config.py epsilon
+
+
+def build(force=False):
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(
+            os.path.join(HERE, "de_oracle.c")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int64)
+
+
+class _OrcDomain(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int64), ("B", ctypes.c_int64),
+        ("g", ctypes.c_double), ("epsilon", ctypes.c_double),
+        ("minimum_allowed_height", ctypes.c_double), ("H0", ctypes.c_double),
+        ("beta_w", ctypes.c_double), ("beta_w_dry", ctypes.c_double),
+        ("beta_uh", ctypes.c_double), ("beta_uh_dry", ctypes.c_double),
+        ("beta_vh", ctypes.c_double), ("beta_vh_dry", ctypes.c_double),
+        ("extrapolate_velocity_second_order", ctypes.c_int64),
+        ("low_froude", ctypes.c_int64),
+        ("ncol_riverwall_hydraulic_properties", ctypes.c_int64),
+        ("neighbours", _ip), ("neighbour_edges", _ip), ("surrogate_neighbours", _ip),
+        ("number_of_boundaries", _ip), ("tri_full_flag", _ip),
+        ("normals", _dp), ("edgelengths", _dp), ("radii", _dp), ("areas", _dp),
+        ("edge_coordinates", _dp), ("centroid_coordinates", _dp),
+        ("edge_flux_type", _ip), ("edge_river_wall_counter", _ip), ("riverwall_rowIndex", _ip),
+        ("riverwall_elevation", _dp), ("riverwall_hydraulic_properties", _dp),
+        ("stage_c", _dp), ("xmom_c", _dp), ("ymom_c", _dp), ("bed_c", _dp), ("height_c", _dp),
+        ("stage_e", _dp), ("xmom_e", _dp), ("ymom_e", _dp), ("bed_e", _dp), ("height_e", _dp),
+        ("stage_v", _dp), ("xmom_v", _dp), ("ymom_v", _dp), ("bed_v", _dp), ("height_v", _dp),
+        ("stage_b", _dp), ("xmom_b", _dp), ("ymom_b", _dp),
+        ("stage_x", _dp), ("xmom_x", _dp), ("ymom_x", _dp),
+        ("stage_s", _dp), ("xmom_s", _dp), ("ymom_s", _dp),
+        ("max_speed", _dp), ("x_work", _dp), ("y_work", _dp),
+        ("boundary_flux_sum", _dp),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.orc_protect.restype = ctypes.c_double
+        L.orc_protect.argtypes = [ctypes.POINTER(_OrcDomain), ctypes.c_int]
+        L.orc_extrapolate.restype = ctypes.c_int
+        L.orc_extrapolate.argtypes = [ctypes.POINTER(_OrcDomain)]
+        L.orc_compute_fluxes.restype = ctypes.c_double
+        L.orc_compute_fluxes.argtypes = [ctypes.POINTER(_OrcDomain), ctypes.c_int64, ctypes.c_double]
+        L.orc_manning_flat.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int64] + [_dp] * 7
+        L.orc_manning_sloped.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int64] + [_dp] * 8
+        L.orc_update.restype = ctypes.c_int
+        L.orc_update.argtypes = [ctypes.c_int64, ctypes.c_double, _dp, _dp, _dp]
+        L.orc_fix_negative.restype = ctypes.c_int64
+        L.orc_fix_negative.argtypes = [ctypes.POINTER(_OrcDomain)]
+        L.orc_backup.argtypes = [ctypes.c_int64, _dp, _dp]
+        L.orc_saxpy.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_double, _dp, _dp]
+        L.orc_bc_reflective.argtypes = [ctypes.POINTER(_OrcDomain), _ip, ctypes.c_int64, _ip, _ip]
+        L.orc_bc_transmissive.argtypes = [ctypes.POINTER(_OrcDomain), _ip, ctypes.c_int64, _ip, _ip, ctypes.c_int]
+        L.orc_bc_dirichlet.argtypes = [ctypes.POINTER(_OrcDomain), _ip, ctypes.c_int64] + [ctypes.c_double] * 3
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def _p(a):
+    if a is None:
+        return None
+    if a.dtype == np.float64:
+        return a.ctypes.data_as(_dp)
+    return a.ctypes.data_as(_ip)
+
+
+# Algorithm defaults, shallow_water/shallow_water_domain.py:583-707
+FLOW_DEFAULTS = {
+    "DE0": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
+                beta_w=0.5, beta_w_dry=0.0, beta_uh=0.5, beta_uh_dry=0.0, beta_vh=0.5, beta_vh_dry=0.0),
+    "DE1": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-5,
+                beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+}
+
+
+class OracleDomain:
+    """A DE0/DE1 domain advanced by the CPU oracle.
+
+    ``mesh`` is any object with the reference's mesh attributes (the
+    product's ``anuga_core_gb300.mesh.Mesh`` or a reference ``Domain``).
+    ``boundaries`` is a list of ``(ids, kind, values)`` with kind in
+    ``reflective``, ``transmissive``, ``transmissive_centroid``,
+    ``dirichlet``.  ``rates`` is a list of ``(indices or None, rate, factor)``.
+    """
+
+    def __init__(self, mesh, flow_algorithm="DE0", protect_zero_ymom=False,
+                 use_sloped_mannings=False, low_froude=0, g=9.8):
+        N = len(mesh)
+        self.N = N
+        self.B = B = int(mesh.boundary_length)
+        d = FLOW_DEFAULTS[flow_algorithm]
+        self.flow_algorithm = flow_algorithm
+        self.CFL = d["CFL"]
+        self.timestepping_method = d["timestepping_method"]
+        self.timestep_fluxcalls = 1 if self.timestepping_method == "euler" else 2
+        self.evolve_max_timestep = 1.0e3    # anuga/config.py max_timestep
+        self.evolve_min_timestep = 1.0e-6   # anuga/config.py min_timestep
+        self.max_smallsteps = 50
+        self.protect_zero_ymom = protect_zero_ymom
+        self.use_sloped_mannings = use_sloped_mannings
+        c = lambda a, t=np.float64: np.ascontiguousarray(a, dtype=t)
+        self.neighbours = c(mesh.neighbours, np.int64).ravel()
+        self.neighbour_edges = c(mesh.neighbour_edges, np.int64).ravel()
+        self.surrogate_neighbours = c(mesh.surrogate_neighbours, np.int64).ravel()
+        self.number_of_boundaries = c(mesh.number_of_boundaries, np.int64)
+        self.tri_full_flag = np.ones(N, np.int64)
+        self.normals = c(mesh.normals).ravel()
+        self.edgelengths = c(mesh.edgelengths).ravel()
+        self.radii = c(mesh.radii)
+        self.areas = c(mesh.areas)
+        self.edge_coordinates = c(mesh.edge_midpoint_coordinates).ravel()
+        self.centroid_coordinates = c(mesh.centroid_coordinates).ravel()
+        self.vertex_coordinates = c(mesh.vertex_coordinates).ravel()
+        self.boundary_cells = c(mesh.boundary_cells, np.int64)
+        self.boundary_edges = c(mesh.boundary_edges, np.int64)
+        z = lambda n: np.zeros(n, np.float64)
+        for q in ("stage", "xmom", "ymom", "bed", "height"):
+            setattr(self, q + "_c", z(N))
+            setattr(self, q + "_e", z(3 * N))
+            setattr(self, q + "_v", z(3 * N))
+        for q in ("stage", "xmom", "ymom"):
+            setattr(self, q + "_b", z(B))
+            setattr(self, q + "_x", z(N))
+            setattr(self, q + "_s", z(N))
+            setattr(self, q + "_0", z(N))
+        self.friction_c = z(N)
+        self.max_speed = z(N)
+        self.x_work = z(N)
+        self.y_work = z(N)
+        self.boundary_flux_sum = z(3)
+        self.D = D = _OrcDomain()
+        D.N, D.B = N, B
+        D.g, D.epsilon = g, EPSILON
+        D.minimum_allowed_height = d["minimum_allowed_height"]
+        D.H0 = 1.0e-5
+        for k in ("beta_w", "beta_w_dry", "beta_uh", "beta_uh_dry", "beta_vh", "beta_vh_dry"):
+            setattr(D, k, d[k])
+        D.extrapolate_velocity_second_order = 1
+        D.low_froude = low_froude
+        for name in ("neighbours", "neighbour_edges", "surrogate_neighbours", "number_of_boundaries",
+                     "tri_full_flag", "normals", "edgelengths", "radii", "areas", "edge_coordinates",
+                     "centroid_coordinates", "stage_c", "xmom_c", "ymom_c", "bed_c", "height_c",
+                     "stage_e", "xmom_e", "ymom_e", "bed_e", "height_e", "stage_v", "xmom_v",
+                     "ymom_v", "bed_v", "height_v", "stage_b", "xmom_b", "ymom_b", "stage_x",
+                     "xmom_x", "ymom_x", "stage_s", "xmom_s", "ymom_s", "max_speed", "x_work",
+                     "y_work", "boundary_flux_sum"):
+            setattr(D, name, _p(getattr(self, name)))
+        self.Dp = ctypes.pointer(D)
+        self.boundaries = []
+        self.rates = []
+        self.relative_time = 0.0
+        self.starttime = 0.0
+        self.timestep = 0.0
+        self.flux_timestep = 0.0
+        self.smallsteps = 0
+        self._order_ = 2
+        self.default_order = 2
+        self.number_of_steps = 0
+        self.total_steps = 0
+        self.evolved_called = False
+        self.timesteps = []
+        self.negative_cells = 0
+
+    @property
+    def minimum_allowed_height(self):
+        return self.D.minimum_allowed_height
+
+    # --- state -------------------------------------------------------------
+    def set_centroid_state(self, stage, xmom, ymom, elevation, friction):
+        self.stage_c[:] = stage
+        self.xmom_c[:] = xmom
+        self.ymom_c[:] = ymom
+        self.bed_c[:] = elevation
+        self.friction_c[:] = friction
+
+    def set_bed_vertex_values(self, zv):
+        self.bed_v[:] = np.asarray(zv, np.float64).ravel()
+
+    def set_boundaries(self, boundaries):
+        self.boundaries = [(np.ascontiguousarray(ids, np.int64), kind, vals)
+                           for ids, kind, vals in boundaries]
+
+    def add_rate(self, indices, rate, factor=1.0):
+        idx = None if indices is None else np.asarray(indices, np.int64)
+        self.rates.append([idx, float(rate), float(factor), 0.0])
+
+    # --- phases ------------------------------------------------------------
+    def protect(self):
+        return lib().orc_protect(self.Dp, 1 if self.protect_zero_ymom else 0)
+
+    def extrapolate(self):
+        lib().orc_extrapolate(self.Dp)
+
+    def distribute_to_vertices_and_edges(self):
+        m = self.protect()
+        self.extrapolate()
+        return m
+
+    def update_boundary(self):
+        L = lib()
+        for ids, kind, vals in self.boundaries:
+            if kind == "reflective":
+                L.orc_bc_reflective(self.Dp, _p(ids), ids.size, _p(self.boundary_cells), _p(self.boundary_edges))
+            elif kind in ("transmissive", "transmissive_centroid"):
+                L.orc_bc_transmissive(self.Dp, _p(ids), ids.size, _p(self.boundary_cells),
+                                      _p(self.boundary_edges), 1 if kind == "transmissive_centroid" else 0)
+            elif kind == "dirichlet":
+                w, uh, vh = (float(v) for v in vals)
+                L.orc_bc_dirichlet(self.Dp, _p(ids), ids.size, w, uh, vh)
+            else:
+                raise ValueError("unknown boundary kind %r" % kind)
+
+    def compute_fluxes(self, substep):
+        self.flux_timestep = lib().orc_compute_fluxes(self.Dp, substep, self.evolve_max_timestep)
+        return self.flux_timestep
+
+    def compute_forcing_terms(self):
+        L = lib()
+        if self.use_sloped_mannings:
+            L.orc_manning_sloped(self.D.g, self.D.minimum_allowed_height, self.N, _p(self.vertex_coordinates),
+                                 _p(self.stage_c), _p(self.bed_v), _p(self.xmom_c), _p(self.ymom_c),
+                                 _p(self.friction_c), _p(self.xmom_s), _p(self.ymom_s))
+        else:
+            L.orc_manning_flat(self.D.g, self.D.minimum_allowed_height, self.N, _p(self.stage_c),
+                               _p(self.bed_c), _p(self.xmom_c), _p(self.ymom_c), _p(self.friction_c),
+                               _p(self.xmom_s), _p(self.ymom_s))
+
+    def update_conserved_quantities(self):
+        L = lib()
+        for q in ("stage", "xmom", "ymom"):
+            err = L.orc_update(self.N, self.timestep, _p(getattr(self, q + "_c")),
+                               _p(getattr(self, q + "_x")), _p(getattr(self, q + "_s")))
+            if err != 0:
+                raise RuntimeError("update: non-positive semi-implicit denominator")
+        self.negative_cells += L.orc_fix_negative(self.Dp)
+
+    def backup(self):
+        for q in ("stage", "xmom", "ymom"):
+            lib().orc_backup(self.N, _p(getattr(self, q + "_c")), _p(getattr(self, q + "_0")))
+
+    def saxpy(self, a, b):
+        for q in ("stage", "xmom", "ymom"):
+            lib().orc_saxpy(self.N, a, b, _p(getattr(self, q + "_c")), _p(getattr(self, q + "_0")))
+
+    def update_timestep(self, yieldstep, finaltime):
+        timestep = min(self.CFL * self.flux_timestep, self.evolve_max_timestep)
+        if timestep < self.evolve_min_timestep:
+            self.smallsteps += 1
+            if self.smallsteps > self.max_smallsteps:
+                self.smallsteps = 0
+                if self._order_ == 1:
+                    raise RuntimeError("Too small timestep %.16f reached" % timestep)
+                self._order_ = 1
+        else:
+            self.smallsteps = 0
+            if self._order_ == 1 and self.default_order == 2:
+                self._order_ = 2
+        if self.relative_finaltime is not None and self.relative_time + timestep > self.relative_finaltime:
+            timestep = self.relative_finaltime - self.relative_time
+        if self.relative_time + timestep > self.relative_yieldtime:
+            timestep = self.relative_yieldtime - self.relative_time
+        self.timestep = timestep
+
+    def apply_fractional_steps(self):
+        for r in self.rates:
+            idx, rate, factor = r[0], r[1], r[2]
+            if rate >= 0.0:
+                local = factor * self.timestep * rate
+                if idx is None:
+                    self.stage_c[:] = self.stage_c[:] + local
+                else:
+                    self.stage_c[idx] = self.stage_c[idx] + local
+            else:
+                sel = slice(None) if idx is None else idx
+                heights = self.stage_c[sel] - self.bed_c[sel]
+                local = np.maximum(factor * self.timestep * rate, -heights)
+                fac = np.where(local < 0.0, (local + heights) / (heights + 1.0e-10), 1.0)
+                self.stage_c[sel] = self.stage_c[sel] + local
+                self.xmom_c[sel] = self.xmom_c[sel] * fac
+                self.ymom_c[sel] = self.ymom_c[sel] * fac
+
+    def euler_step(self, yieldstep, finaltime):
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(0)
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+
+    def rk2_step(self, yieldstep, finaltime):
+        self.backup()
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(0)
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+        self.relative_time = self.relative_time + self.timestep
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(1)
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy(0.5, 0.5)
+
+    def evolve(self, yieldstep=None, finaltime=None, max_steps=None):
+        """Generator with the reference's yield semantics; ``max_steps``
+        stops after that many steps (the step-count form of the benchmark)."""
+        if yieldstep is None:
+            yieldstep = self.evolve_max_timestep
+        yieldstep = float(yieldstep)
+        skip_initial = self.evolved_called
+        self.evolved_called = True
+        self.relative_finaltime = None if finaltime is None else float(finaltime) - self.starttime
+        self.relative_yieldtime = self.relative_time + yieldstep
+        self.number_of_steps = 0
+        if not skip_initial:
+            self.distribute_to_vertices_and_edges()
+            self.update_boundary()
+            yield self.relative_time
+        while True:
+            t0 = self.relative_time
+            if self.timestepping_method == "euler":
+                self.euler_step(yieldstep, finaltime)
+            else:
+                self.rk2_step(yieldstep, finaltime)
+            self.apply_fractional_steps()
+            self.relative_time = t0 + self.timestep
+            self.timesteps.append(self.timestep)
+            self.number_of_steps += 1
+            self.total_steps += 1
+            if max_steps is not None and self.total_steps >= max_steps:
+                self.distribute_to_vertices_and_edges()
+                self.update_boundary()
+                yield self.relative_time
+                return
+            if self.relative_finaltime is not None and self.relative_time >= self.relative_finaltime - EPSILON:
+                if self.relative_time > self.relative_finaltime:
+                    raise RuntimeError("time overshot finaltime")
+                self.relative_time = self.relative_finaltime
+                self.distribute_to_vertices_and_edges()
+                self.update_boundary()
+                yield self.relative_time
+                return
+            if self.relative_time >= self.relative_yieldtime:
+                self.distribute_to_vertices_and_edges()
+                self.update_boundary()
+                yield self.relative_time
+                self.relative_yieldtime += yieldstep
+                self.number_of_steps = 0
+                self.max_speed[:] = 0.0

@@ -1,0 +1,212 @@
+"""Generates the golden fixtures in tests/golden/ from the reference ANUGA.
+
+Run once in a container that has the reference source tree:
+
+    bash tests/golden/build_reference_pkg.sh /path/to/anuga_core
+    OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+
+The reference package is imported from baseline/_ref (built by the script
+above with -ffp-contract=off); the DE kernels run in multiprocessor mode 2
+(OpenMP) with one thread.  Each fixture is a small compressed .npz.
+"""
+import os
+import sys
+
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [os.path.join(ROOT, "baseline", "_ref", "_shims"), os.path.join(ROOT, "baseline", "_ref")]
+
+import numpy as np  # noqa: E402
+import anuga  # noqa: E402
+
+MESH_KEYS = ["vertex_coordinates", "edge_midpoint_coordinates", "centroid_coordinates", "normals",
+             "edgelengths", "areas", "radii", "neighbours", "neighbour_edges", "number_of_boundaries",
+             "surrogate_neighbours", "boundary_cells", "boundary_edges"]
+
+
+def delaunay_case(npts=300, seed=3, size=100.0):
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    pts = rng.uniform(0, size, (npts, 2))
+    tri = Delaunay(pts).simplices.astype(np.int64)
+    a = pts[tri]
+    cr = (a[:, 1, 0] - a[:, 0, 0]) * (a[:, 2, 1] - a[:, 0, 1]) - (a[:, 1, 1] - a[:, 0, 1]) * (a[:, 2, 0] - a[:, 0, 0])
+    tri[cr < 0] = tri[cr < 0][:, [0, 2, 1]]
+    return pts, tri
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+def mesh_fixture(name, points, elements, boundary):
+    d = anuga.Domain(points, elements, boundary)
+    out = {k: np.asarray(getattr(d.mesh, k)) for k in MESH_KEYS}
+    keys = sorted(d.boundary.keys())
+    out["boundary_keys"] = np.array(keys, np.int64).reshape(-1, 2)
+    out["points"] = np.asarray(points, float)
+    out["elements"] = np.asarray(elements, np.int64)
+    save(name, **out)
+
+
+def bumpy_bed(x, y, L):
+    return 0.02 * x - 0.01 * y + 0.6 * np.exp(-((x - 0.4 * L) ** 2 + (y - 0.5 * L) ** 2) / (0.02 * L * L)) \
+        - 0.4 * np.exp(-((x - 0.7 * L) ** 2 + (y - 0.3 * L) ** 2) / (0.01 * L * L))
+
+
+def phase_fixture(name, flow_algorithm, m=8, n=6, L=60.0):
+    """One full set of per-phase outputs from an identical, non-trivial state."""
+    pts, elem, bnd = anuga.rectangular_cross(m, n, L, L * n / m)
+    d = anuga.Domain(pts, elem, bnd)
+    d.set_flow_algorithm(flow_algorithm)
+    d.set_multiprocessor_mode(2)
+    d.set_store(False)
+    d.set_quantity("elevation", lambda x, y: bumpy_bed(x, y, L))
+    d.set_quantity("stage", lambda x, y: np.where(x < 0.45 * L, 1.1, 0.3 + 0.0 * x))
+    rng = np.random.default_rng(11)
+    N = len(d)
+    d.set_quantity("xmomentum", rng.normal(0, 0.05, N), location="centroids")
+    d.set_quantity("ymomentum", rng.normal(0, 0.05, N), location="centroids")
+    d.set_quantity("friction", rng.uniform(0.02, 0.05, N), location="centroids")
+    Br = anuga.Reflective_boundary(d)
+    Bt = anuga.Transmissive_boundary(d)
+    Bd = anuga.Dirichlet_boundary([1.3, 0.05, -0.02])
+    d.set_boundary({"left": Bd, "right": Bt, "top": Br, "bottom": Br})
+    Q = d.quantities
+    out = {}
+
+    def snap(prefix, names):
+        for nm in names:
+            out[prefix + nm] = np.array(nm_arr(nm))
+
+    def nm_arr(nm):
+        q, loc = nm.split(".")
+        return getattr(Q[q], loc)
+
+    cen = ["stage.centroid_values", "xmomentum.centroid_values", "ymomentum.centroid_values",
+           "elevation.centroid_values", "friction.centroid_values", "height.centroid_values"]
+    snap("in.", cen + ["elevation.vertex_values", "elevation.edge_values"])
+    out["in.mass_error"] = np.array(d.protect_against_infinitesimal_and_negative_heights() or 0.0)
+    snap("protect.", cen)
+    from anuga.shallow_water.sw_domain_openmp_ext import extrapolate_second_order_edge_sw
+    extrapolate_second_order_edge_sw(d)
+    edge = [f"{q}.edge_values" for q in ("stage", "xmomentum", "ymomentum", "elevation", "height")]
+    vert = [f"{q}.vertex_values" for q in ("stage", "xmomentum", "ymomentum", "elevation", "height")]
+    snap("extrap.", cen + edge + vert)
+    d.update_boundary()
+    snap("bc.", [f"{q}.boundary_values" for q in ("stage", "xmomentum", "ymomentum")])
+    d.compute_fluxes()
+    out["flux.flux_timestep"] = np.array(d.flux_timestep)
+    out["flux.max_speed"] = np.array(d.max_speed)
+    out["flux.boundary_flux_sum"] = np.array(d.boundary_flux_sum)
+    snap("flux.", [f"{q}.explicit_update" for q in ("stage", "xmomentum", "ymomentum")])
+    d.compute_forcing_terms()
+    snap("forcing.", [f"{q}.semi_implicit_update" for q in ("stage", "xmomentum", "ymomentum")])
+    d.timestep = 0.9 * d.flux_timestep
+    out["update.timestep"] = np.array(d.timestep)
+    d.update_conserved_quantities()
+    snap("update.", cen)
+    out["mesh.points"] = pts
+    out["mesh.elements"] = elem
+    out["params"] = np.array([m, n, L, L * n / m])
+    save(name, **out)
+
+
+def trajectory_fixture(name, build, flow_algorithm, yieldstep, finaltime):
+    d, extra = build()
+    d.set_flow_algorithm(flow_algorithm)
+    d.set_multiprocessor_mode(2)
+    d.set_store(False)
+    out = dict(extra)
+    Q = d.quantities
+    out["init.stage"] = Q["stage"].centroid_values.copy()
+    out["init.xmom"] = Q["xmomentum"].centroid_values.copy()
+    out["init.ymom"] = Q["ymomentum"].centroid_values.copy()
+    out["init.elevation_c"] = Q["elevation"].centroid_values.copy()
+    out["init.elevation_v"] = Q["elevation"].vertex_values.copy()
+    out["init.friction"] = Q["friction"].centroid_values.copy()
+    times, steps, st, xm, ym = [], [], [], [], []
+    for t in d.evolve(yieldstep=yieldstep, finaltime=finaltime):
+        times.append(t)
+        steps.append(d.number_of_steps)
+        st.append(Q["stage"].centroid_values.copy())
+        xm.append(Q["xmomentum"].centroid_values.copy())
+        ym.append(Q["ymomentum"].centroid_values.copy())
+    out["times"] = np.array(times)
+    out["steps"] = np.array(steps)
+    out["stage"] = np.array(st)
+    out["xmom"] = np.array(xm)
+    out["ymom"] = np.array(ym)
+    out["final.stage_edge"] = Q["stage"].edge_values.copy()
+    out["final.stage_vertex"] = Q["stage"].vertex_values.copy()
+    out["yieldstep"] = np.array(yieldstep)
+    out["finaltime"] = np.array(finaltime)
+    save(name, **out)
+
+
+def build_dam_break(m=20):
+    # the small form of the 40,000-triangle dam break (same geometry, coarser mesh)
+    pts, elem, bnd = anuga.rectangular_cross(m, m, 100.0, 100.0)
+    d = anuga.Domain(pts, elem, bnd)
+    d.set_quantity("elevation", lambda x, y: -x / 20)
+    d.set_quantity("stage", lambda x, y: -x / 20 + np.where(x < 50, 1.0, 0.1))
+    d.set_quantity("friction", 0.03)
+    Br = anuga.Reflective_boundary(d)
+    d.set_boundary({"left": Br, "right": Br, "top": Br, "bottom": Br})
+    return d, {"mesh.points": pts, "mesh.elements": elem, "mesh.m": np.array(m)}
+
+
+def build_inflow_bumps(m=16, L=800.0):
+    # the small form of the slope + Gaussian bumps inflow case
+    pts, elem, bnd = anuga.rectangular_cross(m, m, L, L)
+    d = anuga.Domain(pts, elem, bnd)
+    rng = np.random.default_rng(1234)
+    cx = rng.uniform(0, L, 8)
+    cy = rng.uniform(0, L, 8)
+    A = rng.uniform(-5, 5, 8)
+    s = rng.uniform(0.1 * L, 0.4 * L, 8)
+
+    def bed(x, y):
+        z = -0.004 * (x - 0.4 * L)
+        for i in range(8):
+            z = z + A[i] * np.exp(-((x - cx[i]) ** 2 + (y - cy[i]) ** 2) / (2 * s[i] ** 2))
+        return z
+    d.set_quantity("elevation", bed)
+    d.set_quantity("stage", 0.0)
+    N = len(d)
+    d.set_quantity("friction", rng.uniform(0.02, 0.06, N), location="centroids")
+    Br = anuga.Reflective_boundary(d)
+    Bt = anuga.Transmissive_boundary(d)
+    Bd = anuga.Dirichlet_boundary([2.0, 0.0, 0.0])
+    d.set_boundary({"left": Bd, "right": Bt, "top": Br, "bottom": Br})
+    return d, {"mesh.points": pts, "mesh.elements": elem, "mesh.m": np.array(m),
+               "bed.params": np.stack([cx, cy, A, s])}
+
+
+def build_delaunay_rain():
+    pts, tri = delaunay_case(400, seed=5, size=200.0)
+    d = anuga.Domain(pts, tri, None)
+    d.set_quantity("elevation", lambda x, y: 0.01 * x + 0.5 * np.sin(y / 20.0))
+    d.set_quantity("stage", lambda x, y: np.maximum(0.01 * x + 0.5 * np.sin(y / 20.0), 0.3))
+    d.set_quantity("friction", 0.025)
+    Br = anuga.Reflective_boundary(d)
+    d.set_boundary({"exterior": Br})
+    c = d.centroid_coordinates
+    idx = np.nonzero((c[:, 0] > 50) & (c[:, 0] < 150) & (c[:, 1] > 50) & (c[:, 1] < 150))[0]
+    anuga.Rate_operator(d, rate=0.01, indices=idx)
+    return d, {"mesh.points": pts, "mesh.elements": tri, "rain.indices": idx, "rain.rate": np.array(0.01)}
+
+
+if __name__ == "__main__":
+    p, e, b = anuga.rectangular_cross(3, 2, 3.0, 2.0)
+    mesh_fixture("mesh_rect_3x2.npz", p, e, b)
+    p, e = delaunay_case()
+    mesh_fixture("mesh_delaunay_300.npz", p, e, None)
+    phase_fixture("phases_de0.npz", "DE0")
+    phase_fixture("phases_de1.npz", "DE1")
+    trajectory_fixture("traj_dambreak_de0.npz", build_dam_break, "DE0", 1.0, 4.0)
+    trajectory_fixture("traj_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 40.0)
+    trajectory_fixture("traj_delaunay_rain_de1.npz", build_delaunay_rain, "DE1", 2.0, 6.0)
