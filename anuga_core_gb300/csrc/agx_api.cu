@@ -1,0 +1,590 @@
+// agx_api.cu -- C ABI of libagx: scenario lifetime, state access, per-phase
+// calls and the graph-captured device step loop.
+#include "agx_internal.cuh"
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace agx {
+
+static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+static thread_local bool g_capturing = false;
+
+void count_launch(int64_t n) {
+  if (!g_capturing) g_launches += n;
+}
+
+// Event timer used by agx_time_phases: an event after every launch.
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> cat;
+  size_t used = 0;
+};
+static thread_local PhaseTimer* g_timer = nullptr;
+
+void phase_mark(cudaStream_t st, int c) {
+  if (!g_timer) return;
+  PhaseTimer& T = *g_timer;
+  if (T.used == T.ev.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    T.ev.push_back(e);
+    T.cat.push_back(0);
+  }
+  T.cat[T.used] = c;
+  cudaEventRecord(T.ev[T.used], st);
+  T.used++;
+}
+
+static agx_status fail(agx_status code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(AGX_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),   \
+                  __FILE__, __LINE__);                                                  \
+  } while (0)
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Layout of the scenario arena: returns total bytes and (if base != null)
+// assigns the pointers.
+static size_t layout(Scenario* s, char* base) {
+  const size_t N = s->N, B = s->B, E = s->E;
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char* {
+    char* p = base ? base + off : nullptr;
+    off += align_up(bytes ? bytes : 8);
+    return p;
+  };
+  Dev& d = s->d;
+  d.conn = (const int4*)take(N * sizeof(int4));
+  d.surr = (const int4*)take(N * sizeof(int4));
+  d.geo = (const double*)take(N * GEO_STRIDE * 8);
+  d.edge_slot = (const int*)take(E * 4);
+  d.edge_opp = (const int*)take(E * 4);
+  d.normals = (const double*)take(N * 6 * 8);
+  d.lengths = (const double*)take(N * 3 * 8);
+  d.radii = (const double*)take(N * 8);
+  d.areas = (const double*)take(N * 8);
+  d.inv_area = (const double*)take(N * 8);
+  d.vcoord = (const double*)take(N * 6 * 8);
+  d.bslot = (const int*)take(B * 4);
+  s->bkind = (int*)take(B * 4);
+  s->bval = (double*)take(B * 3 * 8);
+  double** cen[] = {&d.w, &d.uh, &d.vh, &d.z, &d.eta, &d.h, &d.u, &d.v, &d.w0, &d.uh0, &d.vh0,
+                    &d.xw, &d.xuh, &d.xvh, &d.sw, &d.suh, &d.svh, &d.max_speed};
+  for (double** p : cen) *p = (double*)take(N * 8);
+  double** edg[] = {&d.we, &d.uhe, &d.vhe, &d.ze, &d.he, &d.wv, &d.uhv, &d.vhv, &d.zv, &d.hv,
+                    &d.sl0, &d.sl1, &d.sl2, &d.slsp, &d.slpf, &d.slhl};
+  for (double** p : edg) *p = (double*)take(N * 3 * 8);
+  double** bnd[] = {&d.wb, &d.uhb, &d.vhb};
+  for (double** p : bnd) *p = (double*)take(B * 8);
+  d.clock = (Clock*)take(sizeof(Clock));
+  return off;
+}
+
+static void bind_fields(Scenario* s) {
+  Dev& d = s->d;
+  const int64_t N = s->N, B = s->B;
+  double* f[AGX_FIELD_COUNT] = {d.w, d.uh, d.vh, d.z, d.eta, d.h, d.we, d.uhe, d.vhe, d.ze, d.he,
+                                d.wv, d.uhv, d.vhv, d.zv, d.hv, d.wb, d.uhb, d.vhb, d.xw, d.xuh,
+                                d.xvh, d.sw, d.suh, d.svh, d.max_speed};
+  for (int i = 0; i < AGX_FIELD_COUNT; i++) {
+    s->field[i] = f[i];
+    int64_t n = N;
+    if (i >= AGX_STAGE_E && i <= AGX_HEIGHT_V) n = 3 * N;
+    if (i >= AGX_STAGE_B && i <= AGX_YMOM_B) n = B;
+    s->field_len[i] = n;
+  }
+}
+
+static void init_clock(Clock* c, const agx_params& p) {
+  memset(c, 0, sizeof(Clock));
+  c->final_time = -1.0;
+  c->yield_time = 1.0e300;
+  c->cfl = p.CFL;
+  c->max_dt = p.evolve_max_timestep;
+  c->min_dt = p.evolve_min_timestep;
+  c->recorded_min = p.evolve_max_timestep;
+  c->recorded_max = p.evolve_min_timestep;
+  c->max_smallsteps = p.max_smallsteps;
+  c->order = 2;
+  c->default_order = 2;
+  c->flux_timestep = p.evolve_max_timestep;
+}
+
+static agx_status sync(Scenario* s) {
+  CK(cudaStreamSynchronize(s->stream));
+  return AGX_OK;
+}
+
+static agx_status pull_clock(Scenario* s) {
+  CK(cudaMemcpyAsync(s->clock_host, s->d.clock, sizeof(Clock), cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+static agx_status push_clock(Scenario* s) {
+  CK(cudaMemcpyAsync(s->d.clock, s->clock_host, sizeof(Clock), cudaMemcpyHostToDevice, s->stream));
+  return sync(s);
+}
+
+static agx_status check_errors(Scenario* s) {
+  const int e = s->clock_host->error;
+  if (e & ERR_NUMERIC) return fail(AGX_E_NUMERIC, "update: non-positive semi-implicit denominator");
+  if (e & ERR_TIMESTEP) return fail(AGX_E_TIMESTEP, "too small timestep reached after %d steps at first order", s->prm.max_smallsteps);
+  if (e & ERR_OVERSHOOT) return fail(AGX_E_OVERSHOOT, "time overshot finaltime");
+  if (e & ERR_NAN) return fail(AGX_E_NUMERIC, "non-finite or non-positive timestep (state diverged)");
+  if (e & ERR_STEPCAP) return fail(AGX_E_STATE, "device loop hit the per-call step cap");
+  return AGX_OK;
+}
+
+static void destroy_graph(Scenario* s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->exec = nullptr;
+  s->graph = nullptr;
+  s->graph_valid = false;
+}
+
+static agx_status build_graph(Scenario* s) {
+  destroy_graph(s);
+  CK(cudaGraphCreate(&s->graph, 0));
+  cudaGraphConditionalHandle handle;
+  CK(cudaGraphConditionalHandleCreate(&handle, s->graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = handle;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, s->graph, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  // capture on the scenario's own stream (the caller's may be the legacy default stream)
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaStreamBeginCaptureToGraph(s->own_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  g_capturing = true;
+  cudaError_t e = enqueue_step(s, s->own_stream, (unsigned long long)handle, true);
+  g_capturing = false;
+  cudaGraph_t captured = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(s->own_stream, &captured);
+  if (e != cudaSuccess) return fail(AGX_E_CUDA, "step capture failed: %s", cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(AGX_E_CUDA, "end capture failed: %s", cudaGetErrorString(e2));
+  CK(cudaGraphInstantiate(&s->exec, s->graph, 0));
+  // kernels per body iteration
+  size_t nn = 0;
+  CK(cudaGraphGetNodes(body, nullptr, &nn));
+  s->kernels_per_step = (int)nn;
+  s->graph_valid = true;
+  return AGX_OK;
+}
+
+}  // namespace agx
+
+struct agx_scenario : public agx::Scenario {};
+
+using namespace agx;
+
+extern "C" {
+
+int32_t agx_version(void) { return 1; }
+
+int64_t agx_kernel_launches(void) { return g_launches.load(); }
+
+int32_t agx_last_error(char* buf, int32_t n) {
+  if (buf && n > 0) {
+    strncpy(buf, g_err, (size_t)n - 1);
+    buf[n - 1] = 0;
+  }
+  return (int32_t)strlen(g_err);
+}
+
+int64_t agx_scenario_footprint(int64_t n_cells, int64_t n_boundary, int64_t n_edges, int32_t precision) {
+  Scenario tmp;
+  tmp.N = (int)n_cells;
+  tmp.B = (int)n_boundary;
+  tmp.E = (int)n_edges;
+  (void)precision;
+  return (int64_t)layout(&tmp, nullptr);
+}
+
+agx_status agx_scenario_create(const agx_mesh_desc* m, const agx_params* p, agx_handle* out) {
+  if (!m || !p || !out) return fail(AGX_E_INVALID, "null argument");
+  *out = nullptr;
+  if (m->n_cells < 0 || m->n_cells >= (1ll << 29) || m->n_boundary < 0 || m->n_edges < 0)
+    return fail(AGX_E_INVALID, "mesh sizes out of range");
+  if (p->timestepping_method != 1 && p->timestepping_method != 2)
+    return fail(AGX_E_INVALID, "timestepping_method must be 1 (euler) or 2 (rk2)");
+  if (p->precision != AGX_PREC_FP64)
+    return fail(AGX_E_INVALID, "this entry point builds the plain FP64 form; use agx_mixed_create for mixed precision");
+  agx_scenario* s = new agx_scenario();
+  s->N = (int)m->n_cells;
+  s->B = (int)m->n_boundary;
+  s->E = (int)m->n_edges;
+  s->prm = *p;
+  CK(cudaGetDevice(&s->device));
+  size_t bytes = layout(s, nullptr);
+  void* arena = nullptr;
+  cudaError_t e = cudaMalloc(&arena, bytes);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(AGX_E_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  s->arena = arena;
+  s->arena_bytes = bytes;
+  layout(s, (char*)arena);
+  bind_fields(s);
+  Params& P = s->d.P;
+  P.g = p->g;
+  P.epsilon = p->epsilon;
+  P.hmin = p->minimum_allowed_height;
+  P.beta_w = p->beta_w;
+  P.beta_w_dry = p->beta_w_dry;
+  P.beta_uh = p->beta_uh;
+  P.beta_uh_dry = p->beta_uh_dry;
+  P.beta_vh = p->beta_vh;
+  P.beta_vh_dry = p->beta_vh_dry;
+  P.c_tmp = 1.0 / (0.3 - 0.1);
+  P.d_tmp = 1.0 - (P.c_tmp * 0.3);
+  P.velocity_extrapolation = p->extrapolate_velocity_second_order == 1;
+  P.low_froude = p->low_froude;
+  P.protect_zero_ymom = p->protect_zero_ymom;
+  P.sloped_mannings = p->use_sloped_mannings;
+  s->d.N = s->N;
+  s->d.B = s->B;
+  s->d.E = s->E;
+  s->d.bkind = s->bkind;
+  s->d.bval = s->bval;
+  s->d.bseries = nullptr;
+  s->d.nseries = 0;
+  *out = s;
+  agx_status st = AGX_OK;
+  auto fin = [&](agx_status code) {
+    agx_scenario_destroy(s);
+    *out = nullptr;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fin(fail(AGX_E_CUDA, "stream create failed"));
+  s->stream = s->own_stream;
+  if (cudaMallocHost(&s->clock_host, sizeof(Clock)) != cudaSuccess) return fin(fail(AGX_E_NOMEM, "pinned clock alloc failed"));
+  if (cudaMemsetAsync(arena, 0, bytes, s->stream) != cudaSuccess) return fin(fail(AGX_E_CUDA, "memset failed"));
+  const size_t N = s->N, B = s->B, E = s->E;
+  struct Up { const void* src; const void* dst; size_t bytes; } ups[] = {
+      {m->conn, s->d.conn, N * 16}, {m->surr, s->d.surr, N * 16}, {m->geo, s->d.geo, N * GEO_STRIDE * 8},
+      {m->edge_slot, s->d.edge_slot, E * 4}, {m->edge_opp, s->d.edge_opp, E * 4},
+      {m->normals, s->d.normals, N * 48}, {m->edgelengths, s->d.lengths, N * 24},
+      {m->radii, s->d.radii, N * 8}, {m->areas, s->d.areas, N * 8}, {m->inv_area, s->d.inv_area, N * 8},
+      {m->vertex_coordinates, s->d.vcoord, N * 48}, {m->boundary_slot, s->d.bslot, B * 4}};
+  for (auto& u : ups) {
+    if (!u.bytes) continue;
+    if (!u.src) return fin(fail(AGX_E_INVALID, "mesh table missing"));
+    if (cudaMemcpyAsync((void*)u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+      return fin(fail(AGX_E_CUDA, "table upload failed"));
+  }
+  init_clock(s->clock_host, *p);
+  if ((st = push_clock(s)) != AGX_OK) return fin(st);
+  return AGX_OK;
+}
+
+agx_status agx_scenario_destroy(agx_handle h) {
+  if (!h) return AGX_OK;
+  agx_scenario* s = h;
+  destroy_graph(s);
+  for (auto& op : s->ops)
+    if (op.idx) cudaFree(op.idx);
+  if (s->bseries) cudaFree(s->bseries);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->own_stream) cudaStreamSynchronize(s->own_stream);
+  if (s->arena) cudaFree(s->arena);
+  if (s->clock_host) cudaFreeHost(s->clock_host);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return AGX_OK;
+}
+
+agx_status agx_set_field(agx_handle h, int32_t f, const double* host, int64_t n) {
+  if (!h || f < 0 || f >= AGX_FIELD_COUNT) return fail(AGX_E_INVALID, "bad handle or field");
+  if (n != h->field_len[f]) return fail(AGX_E_INVALID, "field %d expects %lld values, got %lld", f, (long long)h->field_len[f], (long long)n);
+  if (n == 0) return AGX_OK;
+  CK(cudaMemcpyAsync(h->field[f], host, (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+agx_status agx_get_field(agx_handle h, int32_t f, double* host, int64_t n) {
+  if (!h || f < 0 || f >= AGX_FIELD_COUNT) return fail(AGX_E_INVALID, "bad handle or field");
+  if (n != h->field_len[f]) return fail(AGX_E_INVALID, "field %d holds %lld values, asked for %lld", f, (long long)h->field_len[f], (long long)n);
+  if (n == 0) return AGX_OK;
+  CK(cudaMemcpyAsync(host, h->field[f], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+agx_status agx_device_ptr(agx_handle h, int32_t f, void** ptr, int64_t* n) {
+  if (!h || f < 0 || f >= AGX_FIELD_COUNT || !ptr) return fail(AGX_E_INVALID, "bad handle or field");
+  *ptr = h->field[f];
+  if (n) *n = h->field_len[f];
+  return AGX_OK;
+}
+
+agx_status agx_set_boundary(agx_handle h, const int32_t* kind, const double* values, int64_t B) {
+  if (!h || B != h->B) return fail(AGX_E_INVALID, "boundary arrays must have B=%d entries", h ? h->B : -1);
+  if (B == 0) return AGX_OK;
+  for (int64_t i = 0; i < B; i++)
+    if (kind[i] < AGX_BC_NONE || kind[i] > 6) return fail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
+  CK(cudaMemcpyAsync(h->bkind, kind, (size_t)B * 4, cudaMemcpyHostToDevice, h->stream));
+  if (values) CK(cudaMemcpyAsync(h->bval, values, (size_t)B * 24, cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+agx_status agx_set_boundary_series(agx_handle h, const double* rows, int64_t n_rows) {
+  if (!h || n_rows < 0) return fail(AGX_E_INVALID, "bad arguments");
+  agx_status st = sync(h);
+  if (st) return st;
+  if (h->bseries) cudaFree(h->bseries);
+  h->bseries = nullptr;
+  h->nseries = 0;
+  if (n_rows > 0) {
+    CK(cudaMalloc(&h->bseries, (size_t)n_rows * 32));
+    CK(cudaMemcpyAsync(h->bseries, rows, (size_t)n_rows * 32, cudaMemcpyHostToDevice, h->stream));
+    h->nseries = (int)n_rows;
+  }
+  h->d.bseries = h->bseries;
+  h->d.nseries = h->nseries;
+  h->graph_valid = false;
+  return sync(h);
+}
+
+agx_status agx_add_rate_operator(agx_handle h, const int32_t* indices, int64_t n, double rate, double factor) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  if ((int)h->ops.size() >= MAX_OPS) return fail(AGX_E_INVALID, "at most %d operators", MAX_OPS);
+  RateOp op{nullptr, h->N, rate, factor};
+  if (indices) {
+    for (int64_t i = 0; i < n; i++)
+      if (indices[i] < 0 || indices[i] >= h->N) return fail(AGX_E_INVALID, "operator index %d out of range", indices[i]);
+    op.n = (int)n;
+    if (n > 0) {
+      CK(cudaMalloc(&op.idx, (size_t)n * 4));
+      CK(cudaMemcpyAsync(op.idx, indices, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+  }
+  h->ops.push_back(op);
+  h->graph_valid = false;
+  return sync(h);
+}
+
+agx_status agx_clear_operators(agx_handle h) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = sync(h);
+  if (st) return st;
+  for (auto& op : h->ops)
+    if (op.idx) cudaFree(op.idx);
+  h->ops.clear();
+  h->graph_valid = false;
+  return AGX_OK;
+}
+
+agx_status agx_operator_influx(agx_handle h, int32_t op, double* influx) {
+  if (!h || op < 0 || op >= MAX_OPS || !influx) return fail(AGX_E_INVALID, "bad arguments");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  *influx = h->clock_host->op_influx[op];
+  return AGX_OK;
+}
+
+agx_status agx_protect(agx_handle h, double* mass_error) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  const double before = h->clock_host->mass_added;
+  CK(enqueue_protect(h, h->stream));
+  if ((st = pull_clock(h))) return st;
+  if (mass_error) *mass_error = h->clock_host->mass_added - before;
+  return AGX_OK;
+}
+
+agx_status agx_distribute(agx_handle h, int32_t with_protect) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_distribute(h, h->stream, with_protect != 0, true));
+  return sync(h);
+}
+
+agx_status agx_update_boundary(agx_handle h, double t) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_boundary(h, h->stream, t, false));
+  return sync(h);
+}
+
+agx_status agx_compute_fluxes(agx_handle h, int32_t substep, double* flux_timestep) {
+  if (!h || substep < 0 || substep > 2) return fail(AGX_E_INVALID, "bad arguments");
+  CK(enqueue_fluxes(h, h->stream, substep));
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  Clock* c = h->clock_host;
+  if (substep == 0) {
+    const unsigned long long key = c->dt_key;
+    double v;
+    if (key) {
+      long long bits = (long long)~key;
+      memcpy(&v, &bits, 8);
+    } else {
+      v = 1.0e100;
+    }
+    c->flux_timestep = v;
+  } else {
+    c->flux_timestep = h->prm.evolve_max_timestep;
+  }
+  if ((st = push_clock(h))) return st;
+  if (flux_timestep) *flux_timestep = c->flux_timestep;
+  return AGX_OK;
+}
+
+agx_status agx_compute_forcing(agx_handle h) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_forcing(h, h->stream));
+  return sync(h);
+}
+
+agx_status agx_update_conserved(agx_handle h, double timestep, int64_t* negative_cells) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  const long long before = h->clock_host->negative_cells;
+  CK(enqueue_update(h, h->stream, -1, false, timestep));
+  if ((st = pull_clock(h))) return st;
+  if (negative_cells) *negative_cells = h->clock_host->negative_cells - before;
+  if ((st = check_errors(h))) {
+    h->clock_host->error = 0;
+    push_clock(h);
+    return st;
+  }
+  return AGX_OK;
+}
+
+agx_status agx_backup(agx_handle h) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_backup(h, h->stream));
+  return sync(h);
+}
+
+agx_status agx_saxpy(agx_handle h, double a, double b) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_saxpy(h, h->stream, a, b));
+  return sync(h);
+}
+
+agx_status agx_set_clock(agx_handle h, double time, double yield_time, double final_time) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  Clock* c = h->clock_host;
+  c->time = time;
+  c->yield_time = yield_time;
+  c->final_time = final_time;
+  return push_clock(h);
+}
+
+static void fill_stats(const Clock* c, agx_step_stats* o) {
+  o->time = c->time;
+  o->last_timestep = c->timestep;
+  o->min_timestep = c->recorded_min;
+  o->max_timestep = c->recorded_max;
+  o->flux_timestep = c->flux_timestep;
+  o->mass_added = c->mass_added;
+  for (int i = 0; i < 3; i++) o->boundary_flux_sum[i] = c->bfs[i];
+  o->steps = c->steps_call;
+  o->total_steps = c->total_steps;
+  o->negative_cells = c->negative_cells;
+  o->reason = c->reason;
+  o->order = c->order;
+}
+
+agx_status agx_set_stream(agx_handle h, void* stream) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = sync(h);
+  if (st) return st;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return AGX_OK;
+}
+
+agx_status agx_time_phases(agx_handle h, int32_t reps, double* ms, int32_t n_cat) {
+  if (!h || !ms || reps <= 0 || n_cat < PH_COUNT) return fail(AGX_E_INVALID, "bad arguments");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  Clock saved = *h->clock_host;
+  Clock* c = h->clock_host;
+  c->yield_time = 1.0e300;
+  c->final_time = -1.0;
+  c->steps_target = 0;
+  if ((st = push_clock(h))) return st;
+  for (int i = 0; i < n_cat; i++) ms[i] = 0.0;
+  PhaseTimer T;
+  g_timer = &T;
+  cudaEvent_t start;
+  cudaEventCreate(&start);
+  for (int r = 0; r < reps; r++) {
+    T.used = 0;
+    cudaEventRecord(start, h->stream);
+    cudaError_t e = enqueue_step(h, h->stream, 0ull, false);
+    if (e != cudaSuccess) {
+      g_timer = nullptr;
+      return fail(AGX_E_CUDA, "timed step failed: %s", cudaGetErrorString(e));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    cudaEvent_t prev = start;
+    for (size_t i = 0; i < T.used; i++) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, prev, T.ev[i]);
+      ms[T.cat[i]] += t / reps;
+      prev = T.ev[i];
+    }
+  }
+  g_timer = nullptr;
+  for (auto e : T.ev) cudaEventDestroy(e);
+  cudaEventDestroy(start);
+  // restore the clock bookkeeping (the state itself has advanced)
+  if ((st = pull_clock(h))) return st;
+  c->yield_time = saved.yield_time;
+  c->final_time = saved.final_time;
+  c->steps_target = saved.steps_target;
+  return push_clock(h);
+}
+
+agx_status agx_get_stats(agx_handle h, agx_step_stats* out) {
+  if (!h || !out) return fail(AGX_E_INVALID, "bad arguments");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  fill_stats(h->clock_host, out);
+  return AGX_OK;
+}
+
+agx_status agx_advance(agx_handle h, int64_t max_steps, agx_step_stats* out) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  Clock* c = h->clock_host;
+  c->steps_call = 0;
+  c->steps_target = max_steps > 0 ? max_steps : 0;
+  c->reason = 0;
+  c->recorded_min = h->prm.evolve_max_timestep;
+  c->recorded_max = h->prm.evolve_min_timestep;
+  if ((st = push_clock(h))) return st;
+  if (h->N > 0) {
+    if (!h->graph_valid && (st = build_graph(h)) != AGX_OK) return st;
+    CK(cudaGraphLaunch(h->exec, h->stream));
+  }
+  if ((st = pull_clock(h))) return st;
+  g_launches += (long long)c->steps_call * h->kernels_per_step;
+  if (out) fill_stats(c, out);
+  if ((st = check_errors(h))) return st;
+  return AGX_OK;
+}
+
+}  // extern "C"

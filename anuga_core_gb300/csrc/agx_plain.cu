@@ -1,0 +1,521 @@
+// agx_plain.cu -- FP64 kernels of the DE timestep (plain form, bit-exact).
+//
+// Compiled with --fmad=false: every floating-point operation is rounded on its
+// own, as in the reference built without contraction, so results match the
+// reference's FP64 path bit for bit (Manning's pow excepted: CUDA's and the C
+// library's pow may differ in the last place).
+//
+// One timestep is a fixed sequence of kernels (DE1 = RK2 shown):
+//   prep(backup) -> extrap -> bc -> flux -> accum(dt) -> timestep -> update
+//   -> prep -> extrap -> bc -> flux -> accum -> update(saxpy) -> rates -> clock
+// All state stays in device memory; the clock kernel decides on the device
+// whether another step is needed and sets the graph's while condition.
+#include "agx_internal.cuh"
+#include <cuda_runtime.h>
+
+namespace agx {
+
+constexpr int TPB = 256;
+static const double kNaN = __builtin_nan("");
+
+__device__ __forceinline__ double warp_sum(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_down_sync(0xffffffffu, x, o);
+    x = y > x ? y : x;
+  }
+  return x;
+}
+
+// Block-wide sum, result valid in thread 0.
+__device__ double block_sum(double x) {
+  __shared__ double part[TPB / 32];
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = x;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+__device__ unsigned long long block_max_u64(unsigned long long x) {
+  __shared__ unsigned long long part[TPB / 32];
+  x = warp_max_u64(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = x;
+  __syncthreads();
+  unsigned long long r = 0;
+  if (wid == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0ull;
+    r = warp_max_u64(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// mode bit 0: backup, bit 1: skip protect, bit 2: protect only
+__global__ void k_prep(Dev d, int mode) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double added = 0.0;
+  if (k < d.N) {
+    if (mode & 1) {
+      d.w0[k] = d.w[k];
+      d.uh0[k] = d.uh[k];
+      d.vh0[k] = d.vh[k];
+    }
+    added = prep_cell(d.P, k, d.w, d.uh, d.vh, d.z, d.areas, d.h, d.u, d.v, (mode & 2) == 0,
+                      (mode & 4) == 0);
+  }
+  const int any = __syncthreads_or(added != 0.0);
+  if (any) {
+    const double s = block_sum(added);
+    if (threadIdx.x == 0) atomicAdd(&d.clock->mass_added, s);
+  }
+}
+
+template <bool VERT>
+__global__ void k_extrap(Dev d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  EdgeOut E;
+  const bool sdry = extrap_cell(d.P, k, d.conn, d.surr, d.geo, d.w, d.h, d.u, d.v, E);
+  const size_t b = 3 * (size_t)k;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    d.we[b + i] = E.w[i];
+    d.he[b + i] = E.h[i];
+    d.uhe[b + i] = E.uh[i];
+    d.vhe[b + i] = E.vh[i];
+    d.ze[b + i] = E.z[i];
+  }
+  if (sdry) {
+    d.uh[k] = 0.0;
+    d.vh[k] = 0.0;
+  }
+  if (!VERT && d.P.sloped_mannings) {
+    double vx[3];
+    vertex_from_edges(E.z, vx);   // sloped friction reads the bed vertex values
+    for (int i = 0; i < 3; i++) d.zv[b + i] = vx[i];
+  }
+  if (VERT) {
+    double vx[3];
+    vertex_from_edges(E.w, vx);
+    for (int i = 0; i < 3; i++) d.wv[b + i] = vx[i];
+    vertex_from_edges(E.h, vx);
+    for (int i = 0; i < 3; i++) d.hv[b + i] = vx[i];
+    vertex_from_edges(E.uh, vx);
+    for (int i = 0; i < 3; i++) d.uhv[b + i] = vx[i];
+    vertex_from_edges(E.vh, vx);
+    for (int i = 0; i < 3; i++) d.vhv[b + i] = vx[i];
+    vertex_from_edges(E.z, vx);
+    for (int i = 0; i < 3; i++) d.zv[b + i] = vx[i];
+  }
+}
+
+__device__ void series_value(const double* rows, int n, double t, double out[3]) {
+  if (n <= 0) { out[0] = out[1] = out[2] = 0.0; return; }
+  if (t <= rows[0]) { out[0] = rows[1]; out[1] = rows[2]; out[2] = rows[3]; return; }
+  if (t >= rows[4 * (n - 1)]) {
+    const double* r = rows + 4 * (n - 1);
+    out[0] = r[1]; out[1] = r[2]; out[2] = r[3];
+    return;
+  }
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (rows[4 * mid] <= t) lo = mid; else hi = mid;
+  }
+  const double* a = rows + 4 * lo;
+  const double* c = rows + 4 * hi;
+  const double ratio = (t - a[0]) / (c[0] - a[0]);
+  for (int q = 0; q < 3; q++) out[q] = a[1 + q] + ratio * (c[1 + q] - a[1 + q]);
+}
+
+__global__ void k_bc(Dev d, double t_override, int stage2) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= d.B) return;
+  const int kind = d.bkind[m];
+  if (kind == BK_NONE) return;
+  const int s = d.bslot[m];
+  const int k = s / 3;
+  double tv[3];
+  const double* val = d.bval + 3 * (size_t)m;
+  if (kind == BK_TIME_SERIES) {
+    double t = t_override;
+    if (t != t) t = d.clock->time + (stage2 ? d.clock->timestep : 0.0);  // NaN: use the clock
+    series_value(d.bseries, d.nseries, t, tv);
+    val = tv;
+  }
+  double wb, uhb, vhb;
+  boundary_value(kind, d.normals[2 * s], d.normals[2 * s + 1], d.we[s], d.uhe[s], d.vhe[s], d.w[k],
+                 d.uh[k], d.vh[k], val, wb, uhb, vhb);
+  d.wb[m] = wb;
+  d.uhb[m] = uhb;
+  d.vhb[m] = vhb;
+}
+
+__global__ void k_flux(Dev d) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.E) return;
+  const int s = d.edge_slot[e];
+  const int k = s / 3, i = s - 3 * k;
+  const Riverwall RW = {nullptr, nullptr, nullptr, nullptr, 0};
+  SlotResult R;
+  double hr;
+  slot_flux(d.P, k, i, d.conn[k], d.we, d.uhe, d.vhe, d.ze, d.he, d.wb, d.uhb, d.vhb, d.normals, d.w,
+            d.h, d.z, RW, R, hr);
+  d.sl0[s] = R.f[0];
+  d.sl1[s] = R.f[1];
+  d.sl2[s] = R.f[2];
+  d.slsp[s] = R.speed;
+  d.slpf[s] = R.pflux;
+  d.slhl[s] = R.hleft;
+  const int o = d.edge_opp[e];
+  if (o >= 0) {
+    d.sl0[o] = -R.f[0];
+    d.sl1[o] = -R.f[1];
+    d.sl2[o] = -R.f[2];
+    d.slsp[o] = R.speed;
+    d.slpf[o] = R.pflux;
+    d.slhl[o] = hr;
+  }
+}
+
+__global__ void k_accum(Dev d, int substep) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long key = 0ull;
+  double bflux = 0.0;
+  if (k < d.N) {
+    const int4 c = d.conn[k];
+    SlotResult R[3];
+    int fn[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const size_t s = 3 * (size_t)k + i;
+      R[i].f[0] = d.sl0[s];
+      R[i].f[1] = d.sl1[s];
+      R[i].f[2] = d.sl2[s];
+      R[i].speed = d.slsp[s];
+      R[i].pflux = d.slpf[s];
+      R[i].hleft = d.slhl[s];
+      const int n = i == 0 ? c.x : i == 1 ? c.y : c.z;
+      fn[i] = n >= 0 ? meta_full(d.conn[n].w) : 1;
+    }
+    CellFlux F;
+    accum_cell(d.P, k, c, R, d.he, d.ze, d.h, d.z, d.normals, d.lengths, d.inv_area[k], fn, F);
+    d.xw[k] = F.ew;
+    d.xuh[k] = F.euh;
+    d.xvh[k] = F.evh;
+    bflux = F.bflux;
+    if (substep == 0) {
+      d.max_speed[k] = F.smax;
+      if (F.smax > 0.0) {
+        const double dt = d.radii[k] * 1.0 / F.smax;
+        key = ~(unsigned long long)__double_as_longlong(dt);
+      }
+    }
+  }
+  if (substep == 0) {
+    const unsigned long long bk = block_max_u64(key);
+    if (threadIdx.x == 0 && bk != 0ull) atomicMax(&d.clock->dt_key, bk);
+  }
+  const int any = __syncthreads_or(bflux != 0.0);
+  if (any) {
+    const double bs = block_sum(bflux);
+    if (threadIdx.x == 0) atomicAdd(&d.clock->bfs_acc, bs);
+  }
+}
+
+// update_timestep (generic_domain.py:2349-2415) and the flux_timestep
+// bookkeeping of compute_fluxes; one thread.
+__global__ void k_timestep(Dev d, int substep_count) {
+  Clock* c = d.clock;
+  const unsigned long long key = c->dt_key;
+  const double flux_dt = key ? __longlong_as_double((long long)~key) : 1.0e100;
+  c->flux_timestep = flux_dt;
+  c->bfs[0] = c->bfs_acc;
+  double ts = fmin(c->cfl * flux_dt, c->max_dt);
+  c->recorded_max = fmax(ts, c->recorded_max);
+  c->recorded_min = fmin(ts, c->recorded_min);
+  if (ts < c->min_dt) {
+    c->smallsteps += 1;
+    if (c->smallsteps > c->max_smallsteps) {
+      c->smallsteps = 0;
+      if (c->order == 1) {
+        c->error |= ERR_TIMESTEP;
+        ts = c->min_dt;
+      } else {
+        c->order = 1;
+      }
+    }
+  } else {
+    c->smallsteps = 0;
+    if (c->order == 1 && c->default_order == 2) c->order = 2;
+  }
+  if (c->final_time >= 0.0 && c->time + ts > c->final_time) ts = c->final_time - c->time;
+  if (c->time + ts > c->yield_time) ts = c->yield_time - c->time;
+  c->timestep = ts;
+  (void)substep_count;
+}
+
+__global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int saxpy) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int bad = 0, neg = 0;
+  if (k < d.N) {
+    const double dt = use_clock_dt ? d.clock->timestep : dt_arg;
+    double w = d.w[k], uh = d.uh[k], vh = d.vh[k];
+    const double z = d.z[k];
+    double sw = d.sw[k], suh = d.suh[k], svh = d.svh[k];
+    if (stage >= 0) {   // forcing terms: manning_friction_implicit
+      double S;
+      if (d.P.sloped_mannings) S = manning_S_sloped(d.P, w, d.zv + 3 * (size_t)k, d.vcoord + 6 * (size_t)k, uh, vh, d.eta[k]);
+      else S = manning_S(d.P, w, z, uh, vh, d.eta[k]);
+      suh += S * uh;
+      svh += S * vh;
+    }
+    if (!update_quantity(w, d.xw[k], sw, dt)) bad = 1;
+    if (!update_quantity(uh, d.xuh[k], suh, dt)) bad = 1;
+    if (!update_quantity(vh, d.xvh[k], svh, dt)) bad = 1;
+    if ((w - z < 0.0) & (meta_full(d.conn[k].w) > 0)) {
+      neg = 1;
+      w = z;
+      uh = 0.0;
+      vh = 0.0;
+    }
+    if (saxpy) {
+      w = 0.5 * w + 0.5 * d.w0[k];
+      uh = 0.5 * uh + 0.5 * d.uh0[k];
+      vh = 0.5 * vh + 0.5 * d.vh0[k];
+    }
+    d.w[k] = w;
+    d.uh[k] = uh;
+    d.vh[k] = vh;
+    d.sw[k] = sw;
+    d.suh[k] = suh;
+    d.svh[k] = svh;
+  }
+  const int anyneg = __syncthreads_count(neg);
+  const int anybad = __syncthreads_or(bad);
+  if (threadIdx.x == 0) {
+    if (anyneg) atomicAdd((unsigned long long*)&d.clock->negative_cells, (unsigned long long)anyneg);
+    if (anybad) atomicOr(&d.clock->error, (int)ERR_NUMERIC);
+  }
+}
+
+// Forcing only (per-phase API): accumulate Manning into semi_implicit_update.
+__global__ void k_forcing(Dev d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  const double w = d.w[k], uh = d.uh[k], vh = d.vh[k];
+  double S;
+  if (d.P.sloped_mannings) S = manning_S_sloped(d.P, w, d.zv + 3 * (size_t)k, d.vcoord + 6 * (size_t)k, uh, vh, d.eta[k]);
+  else S = manning_S(d.P, w, d.z[k], uh, vh, d.eta[k]);
+  d.suh[k] += S * uh;
+  d.svh[k] += S * vh;
+}
+
+__global__ void k_backup(Dev d) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  d.w0[k] = d.w[k];
+  d.uh0[k] = d.uh[k];
+  d.vh0[k] = d.vh[k];
+}
+
+__global__ void k_saxpy(Dev d, double a, double b) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  d.w[k] = a * d.w[k] + b * d.w0[k];
+  d.uh[k] = a * d.uh[k] + b * d.uh0[k];
+  d.vh[k] = a * d.vh[k] + b * d.vh0[k];
+}
+
+// Rate_operator with a constant non-negative or negative rate.
+__global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor, int op) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double influx = 0.0;
+  if (j < n) {
+    const int k = idx ? idx[j] : j;
+    const double dt = d.clock->timestep;
+    if (rate >= 0.0) {
+      const double local = factor * dt * rate;
+      d.w[k] = d.w[k] + local;
+      influx = local * d.areas[k];
+    } else {
+      const double height = d.w[k] - d.z[k];
+      const double local = fmax(factor * dt * rate, -height);
+      const double f = local < 0.0 ? (local + height) / (height + 1.0e-10) : 1.0;
+      d.w[k] = d.w[k] + local;
+      d.uh[k] = d.uh[k] * f;
+      d.vh[k] = d.vh[k] * f;
+      influx = local * d.areas[k];
+    }
+  }
+  const int any = __syncthreads_or(influx != 0.0);
+  if (any) {
+    const double s = block_sum(influx);
+    if (threadIdx.x == 0 && op < MAX_OPS) atomicAdd(&d.clock->op_influx[op], s);
+  }
+}
+
+// End of one step (generic_domain.py:1851-1912): advance time, count, and
+// decide whether the device loop continues.
+__global__ void k_clock(Dev d, double t0_unused, cudaGraphConditionalHandle handle, int set_cond) {
+  Clock* c = d.clock;
+  (void)t0_unused;
+  c->time = c->time + c->timestep;
+  c->steps_call += 1;
+  c->total_steps += 1;
+  int reason = 0;
+  // Guards that keep the device loop finite: a NaN time or timestep, a
+  // non-positive timestep, or the per-call step cap end the loop with an error.
+  if (!(c->time == c->time) || !(c->timestep == c->timestep)) c->error |= ERR_NAN;
+  if (!(c->timestep > 0.0) && !(c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) &&
+      !(c->time >= c->yield_time))
+    c->error |= ERR_NAN;
+  if (c->steps_call >= MAX_STEPS_PER_CALL) c->error |= ERR_STEPCAP;
+  if (c->error) {
+    reason = AGX_STOP_ERROR;
+  } else if (c->steps_target > 0 && c->steps_call >= c->steps_target) {
+    reason = AGX_STOP_MAXSTEPS;
+  } else if (c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) {
+    if (c->time > c->final_time) c->error |= ERR_OVERSHOOT;
+    c->time = c->final_time;
+    reason = AGX_STOP_FINAL;
+  } else if (c->time >= c->yield_time) {
+    reason = AGX_STOP_YIELD;
+  }
+  c->reason = reason;
+  if (set_cond) cudaGraphSetConditional(handle, reason == 0 ? 1u : 0u);
+}
+
+// Stage bookkeeping inside an RK2 step: time at stage 2 (set_relative_time).
+__global__ void k_reset_accum(Dev d) {
+  d.clock->dt_key = 0ull;
+  d.clock->bfs_acc = 0.0;
+}
+
+__global__ void k_store_bfs(Dev d, int substep) {
+  d.clock->bfs[substep] = d.clock->bfs_acc;
+  d.clock->bfs_acc = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+static inline int nblk(int n) { return (n + TPB - 1) / TPB; }
+
+#define LAUNCHK(cat, ...)                  \
+  do {                                     \
+    __VA_ARGS__;                           \
+    count_launch();                        \
+    cudaError_t _e = cudaGetLastError();   \
+    if (_e != cudaSuccess) return _e;      \
+    phase_mark(st, cat);                   \
+  } while (0)
+#define LAUNCH(...) LAUNCHK(PH_SMALL, __VA_ARGS__)
+
+cudaError_t enqueue_reset_accum(Scenario* s, cudaStream_t st) {
+  LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(s->d));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_distribute(Scenario* s, cudaStream_t st, bool with_protect, bool vertices) {
+  const Dev& d = s->d;
+  if (d.N == 0) return cudaSuccess;
+  LAUNCHK(PH_PREP, k_prep<<<nblk(d.N), TPB, 0, st>>>(d, with_protect ? 0 : 2));
+  if (vertices) LAUNCHK(PH_EXTRAP, k_extrap<true><<<nblk(d.N), TPB, 0, st>>>(d));
+  else LAUNCHK(PH_EXTRAP, k_extrap<false><<<nblk(d.N), TPB, 0, st>>>(d));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_protect(Scenario* s, cudaStream_t st) {
+  if (s->d.N == 0) return cudaSuccess;
+  LAUNCHK(PH_PREP, k_prep<<<nblk(s->d.N), TPB, 0, st>>>(s->d, 4));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_boundary(Scenario* s, cudaStream_t st, double t_override, bool stage2) {
+  const Dev& d = s->d;
+  if (d.B == 0) return cudaSuccess;
+  LAUNCHK(PH_BC, k_bc<<<nblk(d.B), TPB, 0, st>>>(d, t_override, stage2 ? 1 : 0));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_fluxes(Scenario* s, cudaStream_t st, int substep) {
+  const Dev& d = s->d;
+  if (d.N == 0) return cudaSuccess;
+  LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
+  LAUNCHK(PH_FLUX, k_flux<<<nblk(d.E), TPB, 0, st>>>(d));
+  LAUNCHK(PH_ACCUM, k_accum<<<nblk(d.N), TPB, 0, st>>>(d, substep));
+  LAUNCH(k_store_bfs<<<1, 1, 0, st>>>(d, substep));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_forcing(Scenario* s, cudaStream_t st) {
+  const Dev& d = s->d;
+  if (d.N == 0) return cudaSuccess;
+  LAUNCHK(PH_UPDATE, k_forcing<<<nblk(d.N), TPB, 0, st>>>(d));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_update(Scenario* s, cudaStream_t st, int stage, bool use_clock_dt, double dt) {
+  const Dev& d = s->d;
+  if (d.N == 0) return cudaSuccess;
+  // stage < 0: forcing already accumulated (per-phase API)
+  LAUNCHK(PH_UPDATE, k_update<<<nblk(d.N), TPB, 0, st>>>(d, stage, use_clock_dt ? 1 : 0, dt, 0));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_backup(Scenario* s, cudaStream_t st) {
+  if (s->d.N == 0) return cudaSuccess;
+  LAUNCH(k_backup<<<nblk(s->d.N), TPB, 0, st>>>(s->d));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_saxpy(Scenario* s, cudaStream_t st, double a, double b) {
+  if (s->d.N == 0) return cudaSuccess;
+  LAUNCH(k_saxpy<<<nblk(s->d.N), TPB, 0, st>>>(s->d, a, b));
+  return cudaSuccess;
+}
+
+// One full timestep (Euler or RK2), ending with the clock kernel.
+cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_handle, bool set_cond) {
+  const Dev& d = s->d;
+  const int nb = nblk(d.N), eb = nblk(d.E), bb = nblk(d.B);
+  const bool rk2 = s->prm.timestepping_method == 2;
+  // stage 1
+  LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, rk2 ? 1 : 0));
+  LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
+  if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 0));
+  LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
+  LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
+  LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 0));
+  LAUNCH(k_timestep<<<1, 1, 0, st>>>(d, 0));
+  LAUNCHK(PH_UPDATE, k_update<<<nb, TPB, 0, st>>>(d, 1, 1, 0.0, 0));
+  if (rk2) {
+    LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, 0));
+    LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
+    if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 1));
+    LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
+    LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
+    LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 1));
+    LAUNCH(k_store_bfs<<<1, 1, 0, st>>>(d, 1));
+    LAUNCHK(PH_UPDATE, k_update<<<nb, TPB, 0, st>>>(d, 2, 1, 0.0, 1));
+  }
+  for (size_t i = 0; i < s->ops.size(); i++) {
+    const RateOp& op = s->ops[i];
+    LAUNCHK(PH_RATE, k_rate<<<nblk(op.n), TPB, 0, st>>>(d, op.idx, op.n, op.rate, op.factor, (int)i));
+  }
+  LAUNCH(k_clock<<<1, 1, 0, st>>>(d, 0.0, (cudaGraphConditionalHandle)cond_handle, set_cond ? 1 : 0));
+  return cudaSuccess;
+}
+
+}  // namespace agx

@@ -1,0 +1,808 @@
+"""Drop-in shallow-water Domain whose DE timestep runs on the GPU.
+
+Keeps the user-facing API of the reference's ``anuga.Domain``
+(shallow_water/shallow_water_domain.py:144 and
+abstract_2d_finite_volumes/generic_domain.py): construction from points,
+triangles and a boundary dictionary, ``set_flow_algorithm``,
+``set_quantity``/``get_quantity``, ``set_boundary``, fractional-step
+operators, ``evolve(yieldstep, finaltime|duration)`` as a generator, sww
+output and the per-phase methods (``distribute_to_vertices_and_edges``,
+``update_boundary``, ``compute_fluxes``, ``compute_forcing_terms``,
+``update_timestep``, ``update_conserved_quantities``, ...).
+
+What changes is where the work happens: quantity storage, boundary
+evaluation and the step loop live on the device (libagx), and a whole
+yieldstep runs as one graph launch with a device-side loop.  The host arrays
+behind ``Quantity`` objects are mirrors refreshed on access.
+"""
+from __future__ import annotations
+
+import time
+import warnings
+
+import numpy as np
+
+from . import _lib
+from .mesh import Mesh, rectangular_cross
+from .quantity import Quantity, DEVICE_FIELDS
+from .tables import pack_tables
+
+EPSILON = 1.0e-12        # anuga/config.py:12
+G = 9.8                  # anuga/config.py:45
+MAX_TIMESTEP = 1.0e3     # anuga/config.py:154
+MIN_TIMESTEP = 1.0e-6    # anuga/config.py min_timestep
+MAX_SMALLSTEPS = 50      # anuga/config.py max_smallsteps
+
+# shallow_water_domain.py:583-707
+FLOW_ALGORITHMS = {
+    "DE0": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
+                beta_w=0.5, beta_w_dry=0.0, beta_uh=0.5, beta_uh_dry=0.0, beta_vh=0.5, beta_vh_dry=0.0),
+    "DE1": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-5,
+                beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+}
+
+_STATE_FIELDS = ("stage_c", "xmom_c", "ymom_c")     # pulled eagerly at every yield
+_SYNCED, _DEV_NEWER, _HOST_NEWER = 0, 1, 2
+
+
+def manning_friction_implicit(domain):
+    """Marker for the default forcing term (shallow_water/friction.py:23).  It
+    is evaluated on the device inside the update kernel."""
+    return None
+
+
+class Domain:
+    def __init__(self, coordinates=None, vertices=None, boundary=None, tagged_elements=None,
+                 geo_reference=None, use_inscribed_circle=False, mesh=None, starttime=0.0,
+                 verbose=False, **kwargs):
+        if mesh is None:
+            if coordinates is None or vertices is None:
+                raise ValueError("Domain needs coordinates and vertices (or a mesh)")
+            mesh = Mesh(coordinates, vertices, boundary, use_inscribed_circle=use_inscribed_circle)
+        self.mesh = mesh
+        self.verbose = verbose
+        self.tagged_elements = tagged_elements or {}
+        self.number_of_triangles = self.number_of_elements = len(mesh)
+        self.conserved_quantities = ["stage", "xmomentum", "ymomentum"]
+        self.evolved_quantities = ["stage", "xmomentum", "ymomentum"]
+        self.other_quantities = ["elevation", "friction", "height", "xvelocity", "yvelocity", "x", "y"]
+        self.quantities = {}
+        for name in self.conserved_quantities + self.other_quantities:
+            self.quantities[name] = Quantity(self, name)
+        self._farr = {}
+        for qn, fields in DEVICE_FIELDS.items():
+            Q = self.quantities[qn]
+            for slot, f in zip(("centroid_values", "edge_values", "vertex_values", "boundary_values",
+                                "explicit_update", "semi_implicit_update"), fields):
+                if f is not None:
+                    self._farr[f] = Q._arr[slot]
+        self._farr["max_speed"] = np.zeros(len(mesh))
+        self._fstate = {f: _SYNCED for f in self._farr}
+        self._scn = None
+        self._scn_key = None
+        self.fractional_step_operators = []
+        self.forcing_terms = [manning_friction_implicit]
+        self.boundary_map = None
+        self.boundary_objects = None
+        self.starttime = float(starttime)
+        self.relative_time = 0.0
+        self.evolve_starttime = 0.0
+        self.timestep = 0.0
+        self.flux_timestep = 0.0
+        self.evolved_called = False
+        self.yieldstep_counter = 0
+        self.number_of_steps = 0
+        self.total_steps = 0
+        self.number_of_first_order_steps = 0
+        self.recorded_min_timestep = MAX_TIMESTEP
+        self.recorded_max_timestep = MIN_TIMESTEP
+        self.g = G
+        self.epsilon = EPSILON
+        self.evolve_max_timestep = MAX_TIMESTEP
+        self.evolve_min_timestep = MIN_TIMESTEP
+        self.max_smallsteps = MAX_SMALLSTEPS
+        self.low_froude = 0
+        self.extrapolate_velocity_second_order = True
+        self.use_sloped_mannings = False
+        self.centroid_transmissive_bc = False
+        self.protect_zero_ymom = False
+        self.precision = "fp64"
+        self.multiprocessor_mode = 2
+        self.store = True
+        self.name = "domain"
+        self.datadir = "."
+        self.writer = None
+        self.minimum_storable_height = 1.0e-3
+        self.set_flow_algorithm("DE0")
+        self.quantities["x"].set_values(self.mesh.vertex_coordinates[:, 0].reshape(-1, 3))
+        self.quantities["y"].set_values(self.mesh.vertex_coordinates[:, 1].reshape(-1, 3))
+        self._mass_added_seen = 0.0
+
+    # ------------------------------------------------------------------
+    # mesh accessors
+    def __len__(self):
+        return self.number_of_triangles
+
+    @property
+    def boundary(self):
+        return self.mesh.boundary
+
+    @property
+    def boundary_length(self):
+        return self.mesh.boundary_length
+
+    @property
+    def areas(self):
+        return self.mesh.areas
+
+    @property
+    def normals(self):
+        return self.mesh.normals
+
+    @property
+    def neighbours(self):
+        return self.mesh.neighbours
+
+    @property
+    def centroid_coordinates(self):
+        return self.mesh.centroid_coordinates
+
+    @property
+    def vertex_coordinates(self):
+        return self.mesh.vertex_coordinates
+
+    @property
+    def edge_coordinates(self):
+        return self.mesh.edge_midpoint_coordinates
+
+    @property
+    def tag_boundary_cells(self):
+        return self.mesh.tag_boundary_cells
+
+    @property
+    def boundary_cells(self):
+        return self.mesh.boundary_cells
+
+    @property
+    def boundary_edges(self):
+        return self.mesh.boundary_edges
+
+    def get_centroid_coordinates(self, absolute=False):
+        return self.mesh.centroid_coordinates
+
+    def get_vertex_coordinates(self, absolute=False):
+        return self.mesh.vertex_coordinates
+
+    def get_edge_midpoint_coordinates(self, absolute=False):
+        return self.mesh.edge_midpoint_coordinates
+
+    def get_boundary_tags(self):
+        return self.mesh.get_boundary_tags()
+
+    def get_area(self):
+        return self.mesh.get_area()
+
+    # ------------------------------------------------------------------
+    # configuration
+    def set_flow_algorithm(self, flow_algorithm="DE0"):
+        flow_algorithm = str(flow_algorithm).upper()
+        if flow_algorithm not in FLOW_ALGORITHMS:
+            raise ValueError("flow algorithm %s is not provided (DE0 and DE1 are)" % flow_algorithm)
+        d = FLOW_ALGORITHMS[flow_algorithm]
+        self.flow_algorithm = flow_algorithm
+        self.CFL = d["CFL"]
+        self.timestepping_method = d["timestepping_method"]
+        self.minimum_allowed_height = d["minimum_allowed_height"]
+        for k in ("beta_w", "beta_w_dry", "beta_uh", "beta_uh_dry", "beta_vh", "beta_vh_dry"):
+            setattr(self, k, d[k])
+        self.default_order = 2
+        self._order_ = 2
+        self._invalidate_device()
+
+    def get_flow_algorithm(self):
+        return self.flow_algorithm
+
+    def set_CFL(self, cfl):
+        self.CFL = float(cfl)
+        self._invalidate_device()
+
+    def set_timestepping_method(self, m):
+        m = {1: "euler", 2: "rk2"}.get(m, m)
+        if m not in ("euler", "rk2"):
+            raise ValueError("timestepping method %r not provided (euler, rk2)" % m)
+        self.timestepping_method = m
+        self._invalidate_device()
+
+    def get_timestepping_method(self):
+        return self.timestepping_method
+
+    def set_minimum_allowed_height(self, h):
+        self.minimum_allowed_height = float(h)
+        self._invalidate_device()
+
+    def set_betas(self, beta_w, beta_w_dry, beta_uh, beta_uh_dry, beta_vh, beta_vh_dry):
+        self.beta_w, self.beta_w_dry = beta_w, beta_w_dry
+        self.beta_uh, self.beta_uh_dry = beta_uh, beta_uh_dry
+        self.beta_vh, self.beta_vh_dry = beta_vh, beta_vh_dry
+        self._invalidate_device()
+
+    def set_low_froude(self, low_froude=0):
+        self.low_froude = int(low_froude)
+        self._invalidate_device()
+
+    def set_use_sloped_mannings(self, flag=True):
+        self.use_sloped_mannings = bool(flag)
+        self._invalidate_device()
+
+    def set_centroid_transmissive_bc(self, flag):
+        self.centroid_transmissive_bc = bool(flag)
+        self._bind_boundaries()
+
+    def set_multiprocessor_mode(self, mode=2):
+        """Accepted for compatibility; the DE step always runs on the GPU."""
+        self.multiprocessor_mode = int(mode)
+
+    def set_gpu_options(self, precision=None):
+        if precision is not None:
+            if precision not in ("fp64", "mixed"):
+                raise ValueError("precision must be 'fp64' or 'mixed'")
+            self.precision = precision
+            self._invalidate_device()
+
+    def set_evolve_max_timestep(self, t):
+        self.evolve_max_timestep = float(t)
+        self._invalidate_device()
+
+    def set_store(self, flag=True):
+        self.store = bool(flag)
+
+    def set_name(self, name):
+        self.name = str(name)
+
+    def get_name(self):
+        return self.name
+
+    def set_datadir(self, d):
+        self.datadir = str(d)
+
+    def set_minimum_storable_height(self, h):
+        self.minimum_storable_height = float(h)
+
+    def set_starttime(self, t):
+        self.starttime = float(t)
+
+    def get_time(self):
+        return self.starttime + self.relative_time
+
+    def get_relative_time(self):
+        return self.relative_time
+
+    def set_relative_time(self, t):
+        self.relative_time = float(t)
+
+    def get_timestep(self):
+        return self.timestep
+
+    def get_evolve_starttime(self):
+        return self.evolve_starttime
+
+    # ------------------------------------------------------------------
+    # quantities
+    def get_quantity(self, name):
+        return self.quantities[name]
+
+    def set_quantity(self, name, *args, **kwargs):
+        if "expression" in kwargs:
+            raise NotImplementedError("expression= is not provided; pass an array or function")
+        self.quantities[name].set_values(*args, **kwargs)
+
+    def _quantity_changed(self, name):
+        pass
+
+    def get_conserved_quantities(self, vol_id, vertex=None, edge=None):
+        out = []
+        for n in self.conserved_quantities:
+            Q = self.quantities[n]
+            if edge is not None:
+                out.append(Q.edge_values[vol_id, edge])
+            elif vertex is not None:
+                out.append(Q.vertex_values[vol_id, vertex])
+            else:
+                out.append(Q.centroid_values[vol_id])
+        return np.array(out)
+
+    # ------------------------------------------------------------------
+    # host mirror <-> device synchronisation
+    def _host_view(self, field, arr):
+        if self._scn is not None and self._fstate.get(field) == _DEV_NEWER:
+            self._scn.get(field, out=arr.reshape(-1))
+        if field in self._fstate:
+            # the caller may edit the array in place: send it back before the
+            # next device operation
+            self._fstate[field] = _HOST_NEWER if self._scn is not None else _SYNCED
+
+    def _host_modified(self, field):
+        if field in self._fstate and self._scn is not None:
+            self._fstate[field] = _HOST_NEWER
+
+    def _refresh_velocity(self, Q, slot):
+        src = {"xvelocity": "xmomentum", "yvelocity": "ymomentum"}[Q.name]
+        if slot == "centroid_values":
+            h = self.quantities["height"].centroid_values
+            m = self.quantities[src].centroid_values
+        elif slot == "edge_values":
+            h = self.quantities["height"].edge_values
+            m = self.quantities[src].edge_values
+        else:
+            return
+        with np.errstate(divide="ignore", invalid="ignore"):
+            Q._arr[slot][...] = np.where(h > self.minimum_allowed_height, m / h, 0.0)
+
+    def _push_dirty(self):
+        for f, st in self._fstate.items():
+            if st == _HOST_NEWER:
+                self._scn.set(f, self._farr[f])
+                self._fstate[f] = _SYNCED
+
+    def _mark_device_newer(self, fields=None):
+        for f in (self._fstate if fields is None else fields):
+            self._fstate[f] = _DEV_NEWER
+
+    def _pull(self, fields):
+        for f in fields:
+            if self._fstate[f] == _DEV_NEWER:
+                self._scn.get(f, out=self._farr[f].reshape(-1))
+                self._fstate[f] = _SYNCED
+
+    def _params(self):
+        p = _lib.Params()
+        p.g = self.g
+        p.epsilon = self.epsilon
+        p.minimum_allowed_height = self.minimum_allowed_height
+        for k in ("beta_w", "beta_w_dry", "beta_uh", "beta_uh_dry", "beta_vh", "beta_vh_dry"):
+            setattr(p, k, getattr(self, k))
+        p.CFL = self.CFL
+        p.evolve_max_timestep = self.evolve_max_timestep
+        p.evolve_min_timestep = self.evolve_min_timestep
+        p.extrapolate_velocity_second_order = 1 if self.extrapolate_velocity_second_order else 0
+        p.low_froude = self.low_froude
+        p.timestepping_method = 1 if self.timestepping_method == "euler" else 2
+        p.protect_zero_ymom = 1 if self.protect_zero_ymom else 0
+        p.use_sloped_mannings = 1 if self.use_sloped_mannings else 0
+        p.max_smallsteps = self.max_smallsteps
+        p.precision = _lib.AGX_PREC_FP64 if self.precision == "fp64" else _lib.AGX_PREC_MIXED
+        return p
+
+    def _invalidate_device(self):
+        if self._scn is not None:
+            # keep the device state: pull everything the host may not have yet
+            self._pull([f for f in self._fstate])
+            self._scn.close()
+            self._scn = None
+            for f in self._fstate:
+                self._fstate[f] = _SYNCED
+
+    def _ensure_device(self):
+        if self._scn is not None:
+            return self._scn
+        _lib.require_device()
+        per_side = None
+        if self.low_froude:
+            per_side = np.ones((len(self), 3), bool)
+        if not hasattr(self, "_tables") or self._tables_key != (self.low_froude,):
+            self._tables = pack_tables(self.mesh, per_side_edges=per_side)
+            self._tables_key = (self.low_froude,)
+        if self.precision == "mixed":
+            from .mixed import MixedScenario
+            self._scn = MixedScenario(self.mesh, self._tables, self._params())
+        else:
+            self._scn = _lib.Scenario(self._tables, self._params())
+        up = self._upload_fields()
+        for f in self._fstate:
+            if f in up:
+                self._scn.set(f, self._farr[f])
+            self._fstate[f] = _SYNCED
+        self._bind_boundaries()
+        self._bind_operators()
+        return self._scn
+
+    def _upload_fields(self):
+        return {"stage_c", "xmom_c", "ymom_c", "elev_c", "friction_c", "elev_v",
+                "stage_e", "xmom_e", "ymom_e", "elev_e", "height_e",
+                "stage_b", "xmom_b", "ymom_b", "stage_s", "xmom_s", "ymom_s"}
+
+    def device_tensor(self, name, location="centroids"):
+        """Zero-copy torch view of a device field (the handle outlives it)."""
+        import torch
+        scn = self._ensure_device()
+        self._push_dirty()
+        loc = {"centroids": "_c", "edges": "_e", "vertices": "_v", "boundary": "_b"}[location]
+        field = DEVICE_FIELDS[name][("_c", "_e", "_v", "_b").index(loc)]
+        ptr, n = scn.device_ptr(field)
+        self._fstate[field] = _DEV_NEWER   # the caller may write through the view
+
+        class _CAI:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3}
+        return torch.as_tensor(_CAI(), device="cuda")
+
+    # ------------------------------------------------------------------
+    # boundaries and operators
+    def set_boundary(self, boundary_map):
+        if self.boundary_map is None:
+            self.boundary_map = {}
+        for tag, B in boundary_map.items():
+            if tag not in self.mesh.tag_boundary_cells:
+                raise ValueError("Tag %s provided does not exist in the domain. Boundary tags are %s"
+                                 % (tag, self.get_boundary_tags()))
+            self.boundary_map[tag] = B
+        self.boundary_objects = [(k, self.boundary_map.get(self.mesh.boundary[k])) for k in sorted(self.mesh.boundary)]
+        self._bind_boundaries()
+
+    def _boundary_arrays(self, t):
+        Bn = self.mesh.boundary_length
+        kind = np.zeros(Bn, np.int32)
+        vals = np.zeros((Bn, 3))
+        series = None
+        for tag, ids in self.mesh.tag_boundary_cells.items():
+            B = self.boundary_map.get(tag) if self.boundary_map else None
+            if B is None:
+                continue
+            k = getattr(B, "effective_kind", B.kind)
+            kind[ids] = k
+            if getattr(B, "series", None) is not None:
+                if series is not None and not np.array_equal(series, B.series):
+                    raise NotImplementedError("one time series per domain is supported")
+                series = B.series
+            elif k in (_lib.BC_DIRICHLET, _lib.BC_TRANSMISSIVE_N0):
+                vals[ids] = B.values(t)
+        return kind, vals, series
+
+    def _bind_boundaries(self, t=None):
+        if self._scn is None or self.boundary_map is None:
+            return
+        kind, vals, series = self._boundary_arrays(self.get_time() if t is None else t)
+        self._scn.set_boundary(kind, vals)
+        if series is not None:
+            self._scn.set_boundary_series(series)
+
+    def _operators_changed(self):
+        if self._scn is not None:
+            self._bind_operators()
+
+    def _bind_operators(self):
+        self._scn.clear_operators()
+        self._dev_ops = []
+        for op in self.fractional_step_operators:
+            if getattr(op, "device_loop", False) and hasattr(op, "rate"):
+                self._scn.add_rate(op.indices, op.get_rate(), op.get_factor())
+                self._dev_ops.append(op)
+
+    def _apply_rate_now(self, indices, rate, factor, dt):
+        Q = self.quantities
+        w = Q["stage"].centroid_values
+        sel = slice(None) if indices is None else indices
+        if rate >= 0.0:
+            local = factor * dt * rate
+            w[sel] = w[sel] + local
+        else:
+            heights = w[sel] - Q["elevation"].centroid_values[sel]
+            local = np.maximum(factor * dt * rate, -heights)
+            fac = np.where(local < 0.0, (local + heights) / (heights + 1.0e-10), 1.0)
+            w[sel] = w[sel] + local
+            Q["xmomentum"].centroid_values[sel] *= fac
+            Q["ymomentum"].centroid_values[sel] *= fac
+
+    def _device_loop_ok(self):
+        if self.boundary_map is None:
+            return True
+        for B in self.boundary_map.values():
+            if B is not None and not getattr(B, "device_loop", True):
+                return False
+        for op in self.fractional_step_operators:
+            if not getattr(op, "device_loop", False):
+                return False
+        if any(f is not manning_friction_implicit for f in self.forcing_terms):
+            return False
+        return True
+
+    # ------------------------------------------------------------------
+    # per-phase interface (the reference's plugin surface)
+    def protect_against_infinitesimal_and_negative_heights(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        m = scn.protect()
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c"])
+        return m
+
+    def distribute_to_vertices_and_edges(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        scn.distribute(True)
+        self._mark_device_newer()
+
+    def update_boundary(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        if not self._device_loop_ok():
+            self._bind_boundaries(self.get_time())
+        scn.update_boundary(self.relative_time)
+        self._mark_device_newer(["stage_b", "xmom_b", "ymom_b"])
+
+    def compute_fluxes(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        substep = getattr(self, "_substep", 0)
+        self.flux_timestep = scn.compute_fluxes(substep)
+        self._mark_device_newer(["stage_x", "xmom_x", "ymom_x", "max_speed"])
+
+    def compute_forcing_terms(self):
+        scn = self._ensure_device()
+        for f in self.forcing_terms:
+            if f is manning_friction_implicit:
+                self._push_dirty()
+                scn.compute_forcing()
+                self._mark_device_newer(["xmom_s", "ymom_s"])
+            else:
+                f(self)
+
+    def update_timestep(self, yieldstep, finaltime):
+        """generic_domain.py:2349-2415."""
+        timestep = min(self.CFL * self.flux_timestep, self.evolve_max_timestep)
+        self.recorded_max_timestep = max(timestep, self.recorded_max_timestep)
+        self.recorded_min_timestep = min(timestep, self.recorded_min_timestep)
+        if timestep < self.evolve_min_timestep:
+            self.smallsteps = getattr(self, "smallsteps", 0) + 1
+            if self.smallsteps > self.max_smallsteps:
+                self.smallsteps = 0
+                if self._order_ == 1:
+                    raise RuntimeError("WARNING: Too small timestep %.16f reached even after %d steps "
+                                       "of 1 order scheme" % (timestep, self.max_smallsteps))
+                self._order_ = 1
+        else:
+            self.smallsteps = 0
+            if self._order_ == 1 and self.default_order == 2:
+                self._order_ = 2
+        rf = getattr(self, "relative_finaltime", None)
+        if rf is not None and self.relative_time + timestep > rf:
+            timestep = rf - self.relative_time
+        if self.relative_time + timestep > self.relative_yieldtime:
+            timestep = self.relative_yieldtime - self.relative_time
+        self.timestep = timestep
+
+    def update_conserved_quantities(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        n = scn.update_conserved(self.timestep)
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c", "stage_s", "xmom_s", "ymom_s"])
+        if n > 0:
+            warnings.warn("Negative cells being set to zero depth, possible loss of conservation.")
+        return n
+
+    def backup_conserved_quantities(self):
+        scn = self._ensure_device()
+        self._push_dirty()
+        scn.backup()
+
+    def saxpy_conserved_quantities(self, a, b):
+        scn = self._ensure_device()
+        self._push_dirty()
+        scn.saxpy(a, b)
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c"])
+
+    def apply_fractional_steps(self):
+        for op in self.fractional_step_operators:
+            op()
+
+    def evolve_one_euler_step(self, yieldstep, finaltime):
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 0
+        self.compute_fluxes()
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+
+    def evolve_one_rk2_step(self, yieldstep, finaltime):
+        self.backup_conserved_quantities()
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 0
+        self.compute_fluxes()
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+        self.set_relative_time(self.get_relative_time() + self.timestep)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 1
+        self.compute_fluxes()
+        self._substep = 0
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy_conserved_quantities(0.5, 0.5)
+
+    # ------------------------------------------------------------------
+    # time stepping
+    def _device_steps(self, max_steps=0):
+        scn = self._scn
+        self._push_dirty()
+        rf = self.relative_finaltime if getattr(self, "relative_finaltime", None) is not None else -1.0
+        scn.set_clock(self.relative_time, self.relative_yieldtime, rf)
+        st = scn.advance(max_steps)
+        self._mark_device_newer()
+        self.relative_time = st.time
+        self.timestep = st.last_timestep
+        self.flux_timestep = st.flux_timestep
+        self.number_of_steps += st.steps
+        self.total_steps += st.steps
+        self.recorded_min_timestep = min(self.recorded_min_timestep, st.min_timestep)
+        self.recorded_max_timestep = max(self.recorded_max_timestep, st.max_timestep)
+        self.boundary_flux_sum = np.array(st.boundary_flux_sum[:])
+        self._order_ = st.order
+        self._last_stats = st
+        return st.reason
+
+    def _host_step(self, yieldstep, finaltime):
+        t0 = self.relative_time
+        if self.timestepping_method == "euler":
+            self.evolve_one_euler_step(yieldstep, finaltime)
+        else:
+            self.evolve_one_rk2_step(yieldstep, finaltime)
+        # operators: device ones through the library in one shot
+        for op in self.fractional_step_operators:
+            op()
+        self.relative_time = t0 + self.timestep
+        self.number_of_steps += 1
+        self.total_steps += 1
+        rf = getattr(self, "relative_finaltime", None)
+        if rf is not None and self.relative_time >= rf - EPSILON:
+            if self.relative_time > rf:
+                raise RuntimeError("WARNING (domain.py): time overshot finaltime. ")
+            self.relative_time = rf
+            return _lib.STOP_FINAL
+        if self.relative_time >= self.relative_yieldtime:
+            return _lib.STOP_YIELD
+        return 0
+
+    def evolve(self, yieldstep=None, outputstep=None, finaltime=None, duration=None,
+               skip_initial_step=False):
+        """Generator as in shallow_water_domain.py:2300-2407 / generic_domain.py:1715-1912."""
+        if finaltime is not None:
+            finaltime = float(finaltime)
+        if outputstep is None:
+            outputstep = yieldstep
+        if yieldstep is None:
+            self.output_frequency = 1
+        else:
+            of = outputstep / yieldstep
+            if not float(of).is_integer():
+                raise ValueError("outputstep (%s) should be an integer multiple of yieldstep (%s)"
+                                 % (outputstep, yieldstep))
+            self.output_frequency = int(of)
+        if not (0 <= self.beta_w <= 2.0):
+            raise ValueError("Attribute self.beta_w must be in the interval [0, 2]")
+        self._ensure_device()
+        self.distribute_to_vertices_and_edges()
+        if self.store and (self.relative_time == 0.0 or not self.evolved_called):
+            self._initialise_storage()
+        for t in self._evolve_base(yieldstep, finaltime, duration, skip_initial_step):
+            if self.store and self.yieldstep_counter % self.output_frequency == 0:
+                self.store_timestep()
+            yield t
+            self.yieldstep_counter += 1
+
+    def _evolve_base(self, yieldstep, finaltime, duration, skip_initial_step):
+        if self.boundary_map is None:
+            raise RuntimeError("Boundary tags must be bound to boundary objects before evolving system, "
+                               "e.g. using the method set_boundary. This system has the boundary tags %s"
+                               % self.get_boundary_tags())
+        if self.evolved_called:
+            skip_initial_step = True
+        self.evolved_called = True
+        if skip_initial_step:
+            self.evolve_starttime = self.relative_time
+        if self.relative_time != self.evolve_starttime:
+            self.relative_time = self.evolve_starttime
+        yieldstep = self.evolve_max_timestep if yieldstep is None else float(yieldstep)
+        self.yieldstep = yieldstep
+        self._order_ = self.default_order
+        if finaltime is not None and duration is not None:
+            raise ValueError("Only one of finaltime and duration may be specified")
+        self.relative_finaltime = getattr(self, "relative_finaltime", None)
+        if finaltime is not None:
+            self.finaltime = float(finaltime)
+            self.relative_finaltime = self.finaltime - self.starttime
+        if duration is not None:
+            self.finaltime = float(duration) + self.get_time()
+            self.relative_finaltime = float(duration) + self.relative_time
+        if self.relative_finaltime is not None and self.relative_finaltime < self.relative_time:
+            warnings.warn("finaltime %g is less than current time %g! finaltime set to current time"
+                          % (self.relative_finaltime + self.starttime, self.get_time()))
+            self.relative_finaltime = self.relative_time
+            return
+        self.relative_yieldtime = self.relative_time + yieldstep
+        self.recorded_min_timestep = self.evolve_max_timestep
+        self.recorded_max_timestep = self.evolve_min_timestep
+        self.number_of_steps = 0
+        self.number_of_first_order_steps = 0
+        if not skip_initial_step:
+            self.distribute_to_vertices_and_edges()
+            self.update_boundary()
+            self._pull(_STATE_FIELDS)
+            yield self.get_time()
+        device_loop = self._device_loop_ok()
+        while True:
+            if device_loop:
+                reason = self._device_steps()
+            else:
+                reason = self._host_step(yieldstep, self.relative_finaltime)
+                while reason == 0:
+                    reason = self._host_step(yieldstep, self.relative_finaltime)
+            if reason == _lib.STOP_FINAL:
+                self.relative_time = self.relative_finaltime
+                self.distribute_to_vertices_and_edges()
+                self.update_boundary()
+                self._pull(_STATE_FIELDS)
+                yield self.get_time()
+                break
+            if reason == _lib.STOP_YIELD:
+                self.distribute_to_vertices_and_edges()
+                self.update_boundary()
+                self._pull(_STATE_FIELDS)
+                yield self.get_time()
+                self.relative_yieldtime += yieldstep
+                self.recorded_min_timestep = self.evolve_max_timestep
+                self.recorded_max_timestep = self.evolve_min_timestep
+                self.number_of_steps = 0
+                self.number_of_first_order_steps = 0
+                continue
+            raise RuntimeError("device step loop stopped unexpectedly (reason %d)" % reason)
+
+    def advance_steps(self, n):
+        """Advance exactly n timesteps on the device with no yield or final
+        time (the fixed-step form used for throughput measurement)."""
+        self._ensure_device()
+        if not self._device_loop_ok():
+            raise RuntimeError("advance_steps needs device-evaluable boundaries and operators")
+        self.relative_yieldtime = float("inf")
+        self.relative_finaltime = None
+        reason = self._device_steps(max_steps=int(n))
+        if reason not in (_lib.STOP_MAXSTEPS,):
+            raise RuntimeError("advance_steps stopped early (reason %d)" % reason)
+        return self._last_stats
+
+    # ------------------------------------------------------------------
+    # statistics and output
+    @property
+    def max_speed(self):
+        self._pull(["max_speed"])
+        return self._farr["max_speed"]
+
+    def get_water_volume(self):
+        Q = self.quantities
+        h = Q["stage"].centroid_values - Q["elevation"].centroid_values
+        return float(np.sum(self.mesh.areas * h))
+
+    def timestepping_statistics(self):
+        return ("Time = %.4f, delta t in [%.8f, %.8f], steps=%d"
+                % (self.get_time(), self.recorded_min_timestep, self.recorded_max_timestep,
+                   self.number_of_steps))
+
+    def print_timestepping_statistics(self):
+        print(self.timestepping_statistics())
+
+    def _initialise_storage(self):
+        from .sww import SWW_file
+        self.writer = SWW_file(self)
+        self.writer.store_connectivity()
+
+    def store_timestep(self):
+        if self.writer is not None:
+            self.writer.store_timestep()
+
+
+def rectangular_cross_domain(*args, **kwargs):
+    """anuga.rectangular_cross_domain (anuga/extras.py:13-46)."""
+    verbose = kwargs.pop("verbose", False)
+    points, vertices, boundary = rectangular_cross(*args, **kwargs)
+    return Domain(points, vertices, boundary, verbose=verbose)

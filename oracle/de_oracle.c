@@ -54,6 +54,13 @@ typedef struct {
   double *boundary_flux_sum;              /* [3] per substep */
 } orc_domain;
 
+static int g_parallel_extrapolation = 0;
+
+/* 1: run the extrapolation's main loop with OpenMP like the reference does
+ * (sw_domain_openmp.c:1408), accepting its order dependence; used only for
+ * timing the CPU baseline.  0 (default): index order, the parity semantics. */
+void orc_set_parallel_extrapolation(int on) { g_parallel_extrapolation = on; }
+
 void orc_set_threads(int n) {
 #ifdef _OPENMP
   omp_set_num_threads(n > 0 ? n : 1);
@@ -195,7 +202,8 @@ int orc_extrapolate(orc_domain *D) {
     }
   }
 
-  /* reconstruction, :1418-1896 (in index order) */
+  /* reconstruction, :1418-1896 (in index order unless timing) */
+#pragma omp parallel for schedule(static) if (g_parallel_extrapolation)
   for (k = 0; k < N; k++) {
     const int64_t k3 = 3 * k;
     const double xc = D->centroid_coordinates[2 * k];

@@ -92,12 +92,19 @@ def lib():
         L.orc_bc_dirichlet.argtypes = [ctypes.POINTER(_OrcDomain), _ip, ctypes.c_int64] + [ctypes.c_double] * 3
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_set_parallel_extrapolation.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
 
 
 def set_threads(n):
     lib().orc_set_threads(int(n))
+
+
+def set_parallel_extrapolation(on):
+    """Timing mode: parallel extrapolation loop like the reference's OpenMP
+    build (order-dependent at chunk boundaries); parity runs leave it off."""
+    lib().orc_set_parallel_extrapolation(1 if on else 0)
 
 
 def _p(a):

@@ -1,0 +1,84 @@
+"""The CPU oracle is pinned to the reference: every phase output and three
+full trajectories from the reference ANUGA (tests/golden/, written by
+tests/golden/make_golden.py) are reproduced bit for bit."""
+import numpy as np
+import pytest
+
+from anuga_core_gb300.mesh import Mesh, rectangular_cross
+
+KINDS = {"left": ("dirichlet", (1.3, 0.05, -0.02)), "right": ("transmissive", None),
+         "top": ("reflective", None), "bottom": ("reflective", None)}
+
+
+@pytest.mark.parametrize("alg", ["de0", "de1"])
+def test_oracle_phases_bit_exact(golden, oracle_mod, alg):
+    f = golden("phases_%s.npz" % alg)
+    m, n, L1, L2 = f["params"]
+    p, e, b = rectangular_cross(int(m), int(n), L1, L2)
+    assert np.array_equal(p, f["mesh.points"])
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, alg.upper())
+    od.set_centroid_state(f["in.stage.centroid_values"], f["in.xmomentum.centroid_values"],
+                          f["in.ymomentum.centroid_values"], f["in.elevation.centroid_values"],
+                          f["in.friction.centroid_values"])
+    od.set_boundaries([(M.tag_boundary_cells[t], KINDS[t][0], KINDS[t][1]) for t in M.tag_boundary_cells])
+    od.protect()
+    assert np.array_equal(od.stage_c, f["protect.stage.centroid_values"])
+    assert np.array_equal(od.xmom_c, f["protect.xmomentum.centroid_values"])
+    od.extrapolate()
+    for q, a in [("stage", "stage"), ("xmomentum", "xmom"), ("ymomentum", "ymom"), ("elevation", "bed"),
+                 ("height", "height")]:
+        assert np.array_equal(getattr(od, a + "_e"), f["extrap.%s.edge_values" % q].ravel())
+        assert np.array_equal(getattr(od, a + "_v"), f["extrap.%s.vertex_values" % q].ravel())
+    od.update_boundary()
+    for q, a in [("stage", "stage"), ("xmomentum", "xmom"), ("ymomentum", "ymom")]:
+        assert np.array_equal(getattr(od, a + "_b"), f["bc.%s.boundary_values" % q])
+    assert od.compute_fluxes(0) == float(f["flux.flux_timestep"])
+    assert np.array_equal(od.max_speed, f["flux.max_speed"])
+    assert np.array_equal(od.boundary_flux_sum, f["flux.boundary_flux_sum"])
+    for q, a in [("stage", "stage"), ("xmomentum", "xmom"), ("ymomentum", "ymom")]:
+        assert np.array_equal(getattr(od, a + "_x"), f["flux.%s.explicit_update" % q])
+    od.compute_forcing_terms()
+    for q, a in [("xmomentum", "xmom"), ("ymomentum", "ymom")]:
+        assert np.array_equal(getattr(od, a + "_s"), f["forcing.%s.semi_implicit_update" % q])
+    od.timestep = float(f["update.timestep"])
+    od.update_conserved_quantities()
+    for q, a in [("stage", "stage"), ("xmomentum", "xmom"), ("ymomentum", "ymom")]:
+        assert np.array_equal(getattr(od, a + "_c"), f["update.%s.centroid_values" % q])
+
+
+R = ("reflective", None)
+TRAJ = {
+    "traj_dambreak_de0": ("DE0", {"left": R, "right": R, "top": R, "bottom": R}, False),
+    "traj_inflow_de1": ("DE1", {"left": ("dirichlet", (2.0, 0, 0)), "right": ("transmissive", None),
+                                "top": R, "bottom": R}, False),
+    "traj_delaunay_rain_de1": ("DE1", {"exterior": R}, True),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TRAJ))
+def test_oracle_trajectories_bit_exact(golden, oracle_mod, name):
+    alg, kinds, rain = TRAJ[name]
+    f = golden(name + ".npz")
+    p, e = f["mesh.points"], f["mesh.elements"]
+    b = None
+    if "mesh.m" in f:
+        m = int(f["mesh.m"])
+        L = float(p[:, 0].max())
+        p2, e2, b = rectangular_cross(m, m, L, L)
+        assert np.array_equal(p, p2) and np.array_equal(e, e2)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, alg)
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    od.set_boundaries([(M.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in M.tag_boundary_cells])
+    if rain:
+        od.add_rate(f["rain.indices"], float(f["rain.rate"]))
+    res = [(t, od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy(), od.ymom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["times"])
+    assert [r[1] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[2], f["stage"][i])
+        assert np.array_equal(r[3], f["xmom"][i])
+        assert np.array_equal(r[4], f["ymom"][i])
