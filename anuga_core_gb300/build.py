@@ -26,7 +26,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = [
     ("agx_plain.cu", ["--fmad=false"]),
     ("agx_api.cu", ["--fmad=false"]),
-    ("agx_mixed.cu", []),
+    ("agx_mixed.cu", ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]),
     ("agx_batch.cu", []),
     ("agx_noalloc.cu", ["--fmad=false"]),
 ]

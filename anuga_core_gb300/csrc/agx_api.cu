@@ -25,6 +25,27 @@ struct PhaseTimer {
 };
 static thread_local PhaseTimer* g_timer = nullptr;
 
+void set_capturing(bool on) { g_capturing = on; }
+
+static thread_local PhaseTimer g_shared_timer;
+
+void begin_phase_timer() {
+  g_shared_timer.used = 0;
+  g_timer = &g_shared_timer;
+}
+
+void end_phase_timer(double* ms, int reps, cudaEvent_t start, int abort) {
+  g_timer = nullptr;
+  if (abort || !ms) return;
+  cudaEvent_t prev = start;
+  for (size_t i = 0; i < g_shared_timer.used; i++) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, prev, g_shared_timer.ev[i]);
+    ms[g_shared_timer.cat[i]] += t / reps;
+    prev = g_shared_timer.ev[i];
+  }
+}
+
 void phase_mark(cudaStream_t st, int c) {
   if (!g_timer) return;
   PhaseTimer& T = *g_timer;

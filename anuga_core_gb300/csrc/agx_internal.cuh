@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <string>
 #include <vector>
+#include <cstring>
 #include "../../include/agx.h"
 #include "de_plain.cuh"
 
@@ -30,6 +31,71 @@ struct Clock {
 enum ErrorBits { ERR_NUMERIC = 1, ERR_TIMESTEP = 2, ERR_OVERSHOOT = 4, ERR_NAN = 8, ERR_STEPCAP = 16 };
 // hard cap on the steps one agx_advance call may take on the device
 constexpr long long MAX_STEPS_PER_CALL = 20000000;
+
+// update_timestep (abstract_2d_finite_volumes/generic_domain.py:2349-2415):
+// CFL scaling, small-step fallback to first order, clamp to the final and the
+// next yield time.  Also publishes the flux timestep of the reduction key.
+__host__ __device__ inline void timestep_logic(Clock* c) {
+  const unsigned long long key = c->dt_key;
+  double flux_dt = 1.0e100;
+  if (key) {
+    const unsigned long long bits = ~key;
+    double v;
+    memcpy(&v, &bits, 8);
+    flux_dt = v;
+  }
+  c->flux_timestep = flux_dt;
+  double ts = fmin(c->cfl * flux_dt, c->max_dt);
+  c->recorded_max = fmax(ts, c->recorded_max);
+  c->recorded_min = fmin(ts, c->recorded_min);
+  if (ts < c->min_dt) {
+    c->smallsteps += 1;
+    if (c->smallsteps > c->max_smallsteps) {
+      c->smallsteps = 0;
+      if (c->order == 1) {
+        c->error |= ERR_TIMESTEP;
+        ts = c->min_dt;
+      } else {
+        c->order = 1;
+      }
+    }
+  } else {
+    c->smallsteps = 0;
+    if (c->order == 1 && c->default_order == 2) c->order = 2;
+  }
+  if (c->final_time >= 0.0 && c->time + ts > c->final_time) ts = c->final_time - c->time;
+  if (c->time + ts > c->yield_time) ts = c->yield_time - c->time;
+  c->timestep = ts;
+}
+
+// End of one step (generic_domain.py:1851-1912): advance time, count, and
+// decide whether the loop continues.  Returns the stop reason (0 = go on).
+// Guards keep the device loop finite: a NaN time or timestep, a non-positive
+// timestep or the per-call step cap end it with an error.
+__host__ __device__ inline int clock_logic(Clock* c) {
+  c->time = c->time + c->timestep;
+  c->steps_call += 1;
+  c->total_steps += 1;
+  int reason = 0;
+  if (!(c->time == c->time) || !(c->timestep == c->timestep)) c->error |= ERR_NAN;
+  if (!(c->timestep > 0.0) && !(c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) &&
+      !(c->time >= c->yield_time))
+    c->error |= ERR_NAN;
+  if (c->steps_call >= MAX_STEPS_PER_CALL) c->error |= ERR_STEPCAP;
+  if (c->error) {
+    reason = AGX_STOP_ERROR;
+  } else if (c->steps_target > 0 && c->steps_call >= c->steps_target) {
+    reason = AGX_STOP_MAXSTEPS;
+  } else if (c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) {
+    if (c->time > c->final_time) c->error |= ERR_OVERSHOOT;
+    c->time = c->final_time;
+    reason = AGX_STOP_FINAL;
+  } else if (c->time >= c->yield_time) {
+    reason = AGX_STOP_YIELD;
+  }
+  c->reason = reason;
+  return reason;
+}
 
 struct RateOp {
   int* idx;        // device indices (nullptr: all cells)
@@ -99,6 +165,10 @@ void count_launch(int64_t n = 1);
 // per-kernel event timing (agx_time_phases): categories of step kernels
 enum Phase { PH_PREP = 0, PH_EXTRAP, PH_BC, PH_FLUX, PH_ACCUM, PH_UPDATE, PH_RATE, PH_SMALL, PH_COUNT };
 void phase_mark(cudaStream_t st, int cat);
+void set_capturing(bool on);
+// start collecting events for one timed iteration / accumulate its per-category times
+void begin_phase_timer();
+void end_phase_timer(double* ms, int reps, cudaEvent_t start, int abort);
 
 // implemented in agx_plain.cu
 cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_handle, bool set_cond);

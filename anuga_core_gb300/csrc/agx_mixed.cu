@@ -1,0 +1,1588 @@
+// agx_mixed.cu -- mixed-precision DE step over a pool of scenarios.
+//
+// A pool is one device arena holding many scenarios (meshes of any size).
+// Cells are stored scenario by scenario in space-filling-curve order and
+// grouped into tiles of TILE cells; a tile belongs to one scenario.  Every
+// kernel is persistent (a grid sized to the GPU) and walks the tile table,
+// so one launch advances every active scenario, each with its own timestep,
+// clock and boundary conditions.  A single mixed-precision domain is a pool
+// with one scenario; the batched and serving forms use the same kernels.
+//
+// Per DE1 (RK2) step:
+//   flux1  : FP32 reconstruction + edge fluxes + accumulation, per-scenario
+//            CFL minimum (reduced as FP64 keys)
+//   dt     : update_timestep per scenario (FP64)
+//   update1: FP64 accumulation q1 = protect(q0) + dt E, Manning, fix_negative,
+//            and the FP32 work record for stage 2
+//   flux2  : stage-2 fluxes fused with the update, fix_negative, the RK2
+//            combine 0.5 q0 + 0.5 q2 and the work record of the next step
+//   rates  : Rate_operator stage changes
+//   clock  : per-scenario time bookkeeping; sets the graph's while condition
+// The conserved state (w, uh, vh) and the bed are FP64; the depth w - z is
+// formed in FP64 and rounded once; fluxes and reconstruction are FP32.
+#include "agx_internal.cuh"
+#include "de_mixed.cuh"
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <cstdio>
+#include <map>
+
+namespace agx {
+
+constexpr int TILE = 256;
+
+struct PoolScn {             // device-resident per-scenario record
+  Clock clock;
+  MParams P;
+  int cell0, ncell, tile0, ntile;
+  int bnd0, nbnd;
+  int active, alive;
+  const double* series;      // time series rows (t, w, uh, vh) or null
+  int nseries;
+  int pad[3];
+};
+
+constexpr int HALO_MAX = 256;   // halo cells a tile stages in shared memory
+constexpr int LNK_INLINE = 1023;
+
+struct PoolDev {
+  int ntiles;
+  const int* tile_scn;       // [ntiles] scenario of each tile, -1 = free
+  const int2* tile_halo;     // [ntiles] (offset, count) into halo_cells
+  const int* halo_cells;     // pool cells staged by each tile besides its own
+  const int* lnk;            // per cell: staging index of each slot's neighbour (10 bits each)
+  float2* tile_red1;         // [tiles] stage-1 partials: (min radius/speed, boundary flux)
+  float* tile_red2;          // [tiles] stage-2 boundary flux partials
+  unsigned int* ctl;         // [2] running count and ticket of the clock kernel
+  PoolScn* scn;
+  const int4* conn;          // neighbours (pool-global; boundary -(m+1)) + meta
+  const float4* g0;          // M00 M01 M02 M10
+  const float4* g1;          // M11 M12 M20 M21
+  const float4* g2;          // M22 ex0 ey0 ex1
+  float4* g3;                // ey1 ex2 ey2 radius
+  float4* g4;                // dz0 dz1 dz2 inv_area
+  double *wA, *uhA, *vhA, *wB, *uhB, *vhB, *z;
+  const double* area;
+  float* eta;
+  float4 *W0, *W1;           // work records (h, u, v, -) of stage 1 / stage 2
+  float4* E;                 // explicit update (ew, euh, evh, flags)
+  float* maxs;
+  const int* bkind;
+  const double* bval;
+  const int* bcell;
+};
+
+__device__ __forceinline__ int nb_of(int meta) { return (meta >> 16) & 3; }
+__device__ __forceinline__ int nedge_of(int meta, int i) { return (meta >> (2 * i)) & 3; }
+
+__device__ __forceinline__ float warp_min_f(float x) {
+  for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_down_sync(0xffffffffu, x, o));
+  return x;
+}
+__device__ __forceinline__ double warp_sum_d(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Block reductions (TILE threads); results valid in thread 0.
+__device__ float block_min_f(float x, float* sh) {
+  x = warp_min_f(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = x;
+  __syncthreads();
+  float r = 3.0e38f;
+  if (wid == 0) {
+    r = lane < TILE / 32 ? sh[lane] : 3.0e38f;
+    r = warp_min_f(r);
+  }
+  __syncthreads();
+  return r;
+}
+__device__ double block_sum_d(double x, double* sh) {
+  x = warp_sum_d(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = x;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < TILE / 32 ? sh[lane] : 0.0;
+    r = warp_sum_d(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ---- work record: protect + depth + velocity (FP64 depth, FP32 result) ----
+// protect: sw_domain_openmp.c:1096-1171; preparation: :1373-1402.  Applies
+// the state changes to (w, uh, vh) and returns the work record and the mass
+// added.
+__device__ __forceinline__ float4 protect_prep(const MParams& P, double& w, double& uh, double& vh, double z,
+                                               double area, double& added) {
+  const double depth = w - z;
+  added = 0.0;
+  if (depth < P.hmin64) {
+    uh = 0.0;
+    if (depth <= 0.0 && w < z) {
+      added = (z - w) * area;
+      w = z;
+    }
+  }
+  const double dk = fmax(w - z, 0.0);
+  float4 r;
+  r.x = (float)dk;
+  r.w = 0.0f;
+  if (dk <= P.hmin64) {
+    uh = 0.0;
+    vh = 0.0;
+    r.y = 0.0f;
+    r.z = 0.0f;
+  } else if (P.velocity_extrapolation) {
+    const float inv = 1.0f / r.x;
+    r.y = (float)uh * inv;
+    r.z = (float)vh * inv;
+  } else {
+    r.y = (float)uh;
+    r.z = (float)vh;
+  }
+  return r;
+}
+
+// ---- reconstruction of one cell's three edges (FP32, relative form) -------
+__device__ __forceinline__ void reconstruct(const PoolDev& d, const MParams& P, int c, const float4* W,
+                                            EdgeState out[3], bool& sdry, float4& rc) {
+  const int4 cn = d.conn[c];
+  const int meta = cn.w;
+  const int nb = nb_of(meta);
+  rc = W[c];
+  const int s0 = cn.x >= 0 ? cn.x : c;
+  const int s1 = cn.y >= 0 ? cn.y : c;
+  const int s2 = cn.z >= 0 ? cn.z : c;
+  const float4 r0 = s0 != c ? W[s0] : rc;
+  const float4 r1 = s1 != c ? W[s1] : rc;
+  const float4 r2 = s2 != c ? W[s2] : rc;
+  const float hk = rc.x;
+  sdry = ((r0.x < P.hmin) | (s0 == c)) & ((r1.x < P.hmin) | (s1 == c)) & ((r2.x < P.hmin) | (s2 == c));
+  float uk = rc.y, vk = rc.z;
+  if (sdry) { uk = 0.0f; vk = 0.0f; }
+  const float4 a = d.g0[c], b = d.g1[c], e = d.g2[c], f4 = d.g4[c];
+  const float M[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, e.x};
+  float Dh[3] = {r0.x - hk, r1.x - hk, r2.x - hk};
+  float Dw[3] = {f4.x + Dh[0], f4.y + Dh[1], f4.z + Dh[2]};
+  float Du[3] = {s0 != c ? r0.y - uk : 0.0f, s1 != c ? r1.y - uk : 0.0f, s2 != c ? r2.y - uk : 0.0f};
+  float Dv[3] = {s0 != c ? r0.z - vk : 0.0f, s1 != c ? r1.z - vk : 0.0f, s2 != c ? r2.z - vk : 0.0f};
+  if (s0 == c) { Dh[0] = 0.0f; Dw[0] = 0.0f; }
+  if (s1 == c) { Dh[1] = 0.0f; Dw[1] = 0.0f; }
+  if (s2 == c) { Dh[2] = 0.0f; Dw[2] = 0.0f; }
+  float bw, bu, bv;
+  if (nb <= 1) {
+    const float hlo = fminf(fminf(r0.x, fminf(r1.x, r2.x)), hk);
+    const float hhi = fmaxf(fmaxf(r0.x, fmaxf(r1.x, r2.x)), hk);
+    const float hf = wet_dry_factor32(P, hk, hlo, hhi);
+    bw = P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hf;
+    bu = P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hf;
+    bv = P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hf;
+  } else {
+    bw = bu = bv = (nb == 2) ? P.beta_w : 0.0f;
+  }
+  float Jw[3], Jh[3], Ju[3], Jv[3];
+  limited_jumps(M, Dw, bw, Jw);
+  limited_jumps(M, Dh, bw, Jh);
+  limited_jumps(M, Du, bu, Ju);
+  limited_jumps(M, Dv, bv, Jv);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const float he = hk + Jh[i];
+    const float ue = uk + Ju[i];
+    const float ve = vk + Jv[i];
+    out[i].h = he;
+    if (P.velocity_extrapolation) {
+      out[i].uh = ue * he;
+      out[i].vh = ve * he;
+    } else {
+      out[i].uh = ue;
+      out[i].vh = ve;
+    }
+    out[i].dz = Jw[i] - Jh[i];
+  }
+}
+
+__device__ void series_at(const double* rows, int n, double t, double out[3]) {
+  if (n <= 0 || !rows) { out[0] = out[1] = out[2] = 0.0; return; }
+  if (t <= rows[0]) { out[0] = rows[1]; out[1] = rows[2]; out[2] = rows[3]; return; }
+  if (t >= rows[4 * (n - 1)]) { const double* r = rows + 4 * (n - 1); out[0] = r[1]; out[1] = r[2]; out[2] = r[3]; return; }
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (rows[4 * mid] <= t) lo = mid; else hi = mid;
+  }
+  const double* A = rows + 4 * lo;
+  const double* C = rows + 4 * hi;
+  const double ratio = (t - A[0]) / (C[0] - A[0]);
+  for (int q = 0; q < 3; q++) out[q] = A[1 + q] + ratio * (C[1 + q] - A[1 + q]);
+}
+
+// Manning friction as the factor x with q_new = q_tmp * (1 - x):
+// q_new = q_tmp / (1 - dt S), S = -g eta^2 |q| / h^(7/3)  (sw_domain_openmp.c:1954-1986,
+// quantity.c:772-818).  x = a / (1 + a), a = -dt S >= 0.
+__device__ __forceinline__ float manning_x(const MParams& P, float h, float uh, float vh, float eta, double dt) {
+  if (!(eta > P.hmin) || !(h >= P.hmin)) return 0.0f;
+  const float mom = sqrtf(uh * uh + vh * vh);
+  const float h73 = h * h * cbrtf(h);
+  const float S = P.g * eta * eta * mom / h73;     // -S
+  const float a = (float)dt * S;
+  if (!(a < 1.0e30f)) return 1.0f;
+  return a / (1.0f + a);
+}
+
+// float <-> double conversions done with integer operations on the IEEE-754
+// bit layouts (sign, biased exponent, mantissa), so that they run on the
+// integer pipe instead of the FP64 pipe.  Normal numbers and zero convert
+// exactly (float -> double) or rounded to nearest (double -> float, ties away
+// from zero); values below the float normal range become signed zero.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  const unsigned long long mant = (unsigned long long)(b & 0x7fffffu) << 29;
+  const unsigned long long ex = (e == 255u) ? 2047ull : (unsigned long long)(e + 896u);
+  const unsigned long long r = (e == 0u) ? sign : (sign | (ex << 52) | mant);
+  return __longlong_as_double((long long)r);
+}
+
+__device__ __forceinline__ float d2f_bits(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  b &= 0x7fffffffffffffffull;
+  b += (1ull << 28);
+  const int e = (int)(b >> 52) - 896;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned int)e << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
+}
+
+__device__ __forceinline__ bool negative_bits(double x) { return __double_as_longlong(x) < 0; }
+
+// Work record (depth, velocity) of a state whose depth w - z is `depth`
+// (protect and the preparation of the extrapolation, in FP32 on the depth
+// formed in FP64).
+__device__ __forceinline__ float4 record_of(const MParams& P, double depth, double uh, double vh) {
+  const float h = fmaxf(d2f_bits(depth), 0.0f);
+  float4 r = make_float4(h, 0.0f, 0.0f, 0.0f);
+  if (h > P.hmin) {
+    if (P.velocity_extrapolation) {
+      const float inv = 1.0f / h;
+      r.y = d2f_bits(uh) * inv;
+      r.z = d2f_bits(vh) * inv;
+    } else {
+      r.y = d2f_bits(uh);
+      r.z = d2f_bits(vh);
+    }
+  }
+  return r;
+}
+
+
+// FP64 update of one cell from the stage-start state (w, uh, vh):
+// protect + preparation zeroing (distribute_to_vertices_and_edges), the
+// surrounded-by-dry zeroing, Manning friction with its semi-implicit factor
+// (sw_domain_openmp.c:1954-1986, quantity.c:772-818) and fix_negative_cells.
+// The increments dt*E (and the friction correction) are formed in FP32 and
+// accumulated into the FP64 state with one FP64 add per quantity.
+// Returns 1 if the cell was fixed as negative; depth1 = w - z afterwards.
+__device__ __forceinline__ int update_lean(const MParams& P, double& w, double& uh, double& vh, double z,
+                                           double area, float eta, float4 Ek, double dt, float dt32,
+                                           double& added, double& depth1) {
+  const double depth = w - z;
+  const float h = d2f_bits(depth);
+  added = 0.0;
+  if (h <= P.hmin) {
+    uh = 0.0;
+    vh = 0.0;
+    if (negative_bits(depth)) {
+      added = -depth * area;
+      w = z;
+    }
+  }
+  if (Ek.w != 0.0f) { uh = 0.0; vh = 0.0; }
+  const float uh32 = d2f_bits(uh), vh32 = d2f_bits(vh);
+  const float x = manning_x(P, fmaxf(h, 0.0f), uh32, vh32, eta, dt);
+  const float dw = dt32 * Ek.x;
+  float du = dt32 * Ek.y;
+  float dv = dt32 * Ek.z;
+  du = du - x * (uh32 + du);
+  dv = dv - x * (vh32 + dv);
+  w = w + f2d_bits(dw);
+  uh = uh + f2d_bits(du);
+  vh = vh + f2d_bits(dv);
+  depth1 = w - z;
+  if (negative_bits(depth1)) {
+    w = z;
+    uh = 0.0;
+    vh = 0.0;
+    depth1 = 0.0;
+    return 1;
+  }
+  return 0;
+}
+
+__device__ __forceinline__ float warp_sum_f(float x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+__device__ float block_sum_f(float x, float* sh) {
+  x = warp_sum_f(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = x;
+  __syncthreads();
+  float r = 0.0f;
+  if (wid == 0) {
+    r = lane < TILE / 32 ? sh[lane] : 0.0f;
+    r = warp_sum_f(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Fused flux kernel.  Phase 1 reconstructs the tile's own cells and its halo
+// cells (the outside neighbours its edges need) into shared memory; phase 2
+// evaluates the three edge fluxes of every own cell from shared memory and
+// accumulates them.  FUSED2: stage 2 of RK2 (update and combine fused in).
+template <bool FUSED2>
+__global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
+  __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
+  __shared__ float shf[TILE / 32];
+  __shared__ double shd[TILE / 32];
+  const float4* W = FUSED2 ? d.W1 : d.W0;
+  for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int sid = d.tile_scn[tile];
+    if (sid < 0) continue;
+    PoolScn* S = d.scn + sid;
+    if (!S->active) continue;
+    if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
+    const MParams P = S->P;
+    const int base = tile * TILE;
+    const int k = base + threadIdx.x;
+    const bool valid = k < S->cell0 + S->ncell;
+    bool sdry = false;
+    float4 rk = make_float4(0.f, 0.f, 0.f, 0.f);
+    EdgeState own[3];
+    if (valid) {
+      reconstruct(d, P, k, W, own, sdry, rk);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; i++) own[i] = EdgeState{0.f, 0.f, 0.f, 0.f};
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) es[threadIdx.x * 3 + i] = own[i];
+    const int2 ht = d.tile_halo[tile];
+    for (int h = threadIdx.x; h < ht.y; h += TILE) {
+      EdgeState hs[3];
+      bool sd;
+      float4 rn;
+      reconstruct(d, P, d.halo_cells[ht.x + h], W, hs, sd, rn);
+#pragma unroll
+      for (int i = 0; i < 3; i++) es[(TILE + h) * 3 + i] = hs[i];
+    }
+    __syncthreads();
+    float ew = 0.f, ex = 0.f, ey = 0.f, smax = 0.f, bfl = 0.f;
+    float4 g3 = make_float4(0.f, 0.f, 0.f, 0.f), g4 = g3;
+    if (valid) {
+      const int4 cn = d.conn[k];
+      const int lk = d.lnk[k];
+      const float4 g2 = d.g2[k];
+      g3 = d.g3[k];
+      g4 = d.g4[k];
+      const float evx[3] = {g2.y, g2.w, g3.y};
+      const float evy[3] = {g2.z, g3.x, g3.z};
+      const float dzn[3] = {g4.x, g4.y, g4.z};
+      const int nbr[3] = {cn.x, cn.y, cn.z};
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const EdgeState L = own[i];
+        const int n = nbr[i];
+        float hre, uhr, vhr, dd = 0.0f;
+        const float len = sqrtf(evx[i] * evx[i] + evy[i] * evy[i]);
+        const float il = 1.0f / len;
+        const float n1 = evy[i] * il, n2 = -evx[i] * il;
+        if (n >= 0) {
+          const int m = nedge_of(cn.w, i);
+          const int li = (lk >> (10 * i)) & 1023;
+          EdgeState R;
+          if (li != LNK_INLINE) {
+            R = es[li * 3 + m];
+          } else {      // halo overflow: reconstruct inline
+            EdgeState tmp[3];
+            bool sd;
+            float4 rn;
+            reconstruct(d, P, n, W, tmp, sd, rn);
+            R = m == 0 ? tmp[0] : (m == 1 ? tmp[1] : tmp[2]);
+          }
+          hre = R.h;
+          uhr = R.uh;
+          vhr = R.vh;
+          dd = dzn[i] + R.dz - L.dz;        // zr - zl
+        } else {
+          const int mb = -n - 1;
+          const int kind = d.bkind[mb];
+          const double* bv = d.bval + 3 * (size_t)mb;
+          switch (kind) {
+            case BK_REFLECTIVE: {
+              hre = fmaxf(L.h, 0.0f);
+              const float q1 = L.uh, q2 = L.vh;
+              const float r1 = -q1 * n1 - q2 * n2;
+              const float r2 = -q1 * n2 + q2 * n1;
+              uhr = n1 * r1 - n2 * r2;
+              vhr = n2 * r1 + n1 * r2;
+              break;
+            }
+            case BK_TRANSMISSIVE:
+              hre = fmaxf(L.h, 0.0f);
+              uhr = L.uh;
+              vhr = L.vh;
+              break;
+            case BK_TRANSMISSIVE_C:
+              hre = fmaxf(rk.x - L.dz, 0.0f);
+              uhr = P.velocity_extrapolation ? rk.y * rk.x : rk.y;
+              vhr = P.velocity_extrapolation ? rk.z * rk.x : rk.z;
+              break;
+            case BK_TRANSMISSIVE_N0: {
+              hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
+              const float nq = n1 * L.uh + n2 * L.vh;
+              uhr = nq * n1;
+              vhr = nq * n2;
+              break;
+            }
+            case BK_TIME_SERIES: {
+              double v3[3];
+              const double tnow = S->clock.time + (FUSED2 ? S->clock.timestep : 0.0);
+              series_at(S->series, S->nseries, tnow, v3);
+              hre = fmaxf((float)(v3[0] - d.z[k]) - L.dz, 0.0f);
+              uhr = (float)v3[1];
+              vhr = (float)v3[2];
+              break;
+            }
+            default: {   // Dirichlet, or no boundary object (values stay zero)
+              hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
+              uhr = (float)bv[1];
+              vhr = (float)bv[2];
+              break;
+            }
+          }
+        }
+        Flux32 F;
+        central_flux32(L.h, L.uh, L.vh, hre, uhr, vhr, dd, n1, n2, P, F);
+        const float e0 = -F.f0 * len;
+        const float e1 = -F.f1 * len;
+        const float e2 = -F.f2 * len;
+        const float pg = len * (-P.g * 0.5f * (F.hl * F.hl - L.h * L.h - (L.h + rk.x) * L.dz) + F.pflux);
+        ew += e0;
+        ex += e1;
+        ey += e2;
+        ex -= n1 * pg;
+        ey -= n2 * pg;
+        if (F.speed > P.eps) smax = fmaxf(smax, F.speed);
+        if (n < 0) bfl += e0;
+      }
+      const float ia = g4.w;
+      ew *= ia;
+      ex *= ia;
+      ey *= ia;
+    }
+    if (!FUSED2) {
+      float dtk = 3.0e38f;
+      if (valid) {
+        d.E[k] = make_float4(ew, ex, ey, sdry ? 1.0f : 0.0f);
+        d.maxs[k] = smax;
+        if (smax > 0.0f) dtk = g3.w / smax;
+      }
+      const float bm = block_min_f(dtk, shf);
+      const float bs = block_sum_f(bfl, shf);
+      if (threadIdx.x == 0) d.tile_red1[tile] = make_float2(bm, bs);
+    } else {
+      int neg = 0;
+      double added = 0.0;
+      if (valid) {
+        const double dt = S->clock.timestep;
+        double w = d.wB[k], uh = d.uhB[k], vh = d.vhB[k];
+        const double z = d.z[k];
+        double depth1;
+        neg = update_lean(P, w, uh, vh, z, d.area[k], d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f), dt,
+                          (float)dt, added, depth1);
+        w = 0.5 * w + 0.5 * d.wA[k];
+        uh = 0.5 * uh + 0.5 * d.uhA[k];
+        vh = 0.5 * vh + 0.5 * d.vhA[k];
+        d.wA[k] = w;
+        d.uhA[k] = uh;
+        d.vhA[k] = vh;
+        d.W0[k] = record_of(P, w - z, uh, vh);     // work record of the next step
+      }
+      const float bs = block_sum_f(bfl, shf);
+      const int anym = __syncthreads_or(added != 0.0);
+      const double ma = anym ? block_sum_d(added, shd) : 0.0;
+      const int nneg = __syncthreads_count(neg);
+      if (threadIdx.x == 0) {
+        d.tile_red2[tile] = bs;
+        if (ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
+        if (nneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)nneg);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Stage-1 update (RK2: q1 into B; Euler: in place into A) and the next
+// stage's work record.  One block per tile; warp-level bookkeeping only.
+__global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
+  (void)unused;
+  for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int sid = d.tile_scn[tile];
+    if (sid < 0) continue;
+    PoolScn* S = d.scn + sid;
+    if (!S->active) continue;
+    const MParams P = S->P;
+    const int euler = !P.rk2;
+    const int k = tile * TILE + threadIdx.x;
+    const bool valid = k < S->cell0 + S->ncell;
+    int neg = 0;
+    double added = 0.0;
+    if (valid) {
+      const double dt = S->clock.timestep;
+      double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
+      const double z = d.z[k];
+      double depth1;
+      neg = update_lean(P, w, uh, vh, z, d.area[k], d.eta[k], d.E[k], dt, (float)dt, added, depth1);
+      const float4 r = record_of(P, depth1, uh, vh);
+      if (euler) {
+        d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh;
+        d.W0[k] = r;
+      } else {
+        d.wB[k] = w; d.uhB[k] = uh; d.vhB[k] = vh;
+        d.W1[k] = r;
+      }
+    }
+    const unsigned full = 0xffffffffu;
+    const unsigned nb = __ballot_sync(full, neg);
+    if (__any_sync(full, added != 0.0)) {
+      const double ws = warp_sum_d(added);
+      if ((threadIdx.x & 31) == 0 && ws != 0.0) atomicAdd(&S->clock.mass_added, ws);
+    }
+    if (nb && (threadIdx.x & 31) == 0)
+      atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)__popc(nb));
+  }
+}
+
+// Work record from the state A (after set_field or an operator), optionally
+// applying protect to A in place (distribute_to_vertices_and_edges).
+__global__ void k_pool_prep(PoolDev d, int inplace, int only_scn) {
+  __shared__ double shd[TILE / 32];
+  for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int sid = d.tile_scn[tile];
+    if (sid < 0 || (only_scn >= 0 && sid != only_scn)) continue;
+    PoolScn* S = d.scn + sid;
+    const int k = tile * TILE + threadIdx.x;
+    const bool valid = k < S->cell0 + S->ncell;
+    double added = 0.0;
+    if (valid) {
+      double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
+      d.W0[k] = protect_prep(S->P, w, uh, vh, d.z[k], d.area[k], added);
+      if (inplace) { d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh; }
+    }
+    const double ma = block_sum_d(added, shd);
+    if (threadIdx.x == 0 && inplace && ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
+  }
+}
+
+// Surrounded-by-dry momentum zeroing of the extrapolation (persistent part).
+__global__ void k_pool_sdry(PoolDev d, int only_scn) {
+  for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int sid = d.tile_scn[tile];
+    if (sid < 0 || (only_scn >= 0 && sid != only_scn)) continue;
+    PoolScn* S = d.scn + sid;
+    const int k = tile * TILE + threadIdx.x;
+    if (k >= S->cell0 + S->ncell) continue;
+    const int4 cn = d.conn[k];
+    const float hm = S->P.hmin;
+    const int s0 = cn.x >= 0 ? cn.x : k, s1 = cn.y >= 0 ? cn.y : k, s2 = cn.z >= 0 ? cn.z : k;
+    const bool sd = ((d.W0[s0].x < hm) | (s0 == k)) & ((d.W0[s1].x < hm) | (s1 == k)) & ((d.W0[s2].x < hm) | (s2 == k));
+    if (sd) { d.uhA[k] = 0.0; d.vhA[k] = 0.0; }
+  }
+}
+
+// Bed differences to the surrogate neighbours (after the elevation changes).
+__global__ void k_pool_dz(PoolDev d, int only_scn) {
+  for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int sid = d.tile_scn[tile];
+    if (sid < 0 || (only_scn >= 0 && sid != only_scn)) continue;
+    PoolScn* S = d.scn + sid;
+    const int k = tile * TILE + threadIdx.x;
+    if (k >= S->cell0 + S->ncell) continue;
+    const int4 cn = d.conn[k];
+    const double zk = d.z[k];
+    float4 g = d.g4[k];
+    g.x = cn.x >= 0 ? (float)(d.z[cn.x] - zk) : 0.0f;
+    g.y = cn.y >= 0 ? (float)(d.z[cn.y] - zk) : 0.0f;
+    g.z = cn.z >= 0 ? (float)(d.z[cn.z] - zk) : 0.0f;
+    d.g4[k] = g;
+  }
+}
+
+// Edge and vertex values in FP64 (for output and the Quantity API).
+__global__ void k_pool_edges(PoolDev d, int sid, double* we, double* he, double* uhe, double* vhe, double* ze,
+                             const int* order) {
+  PoolScn* S = d.scn + sid;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= S->ncell) return;
+  const int k = S->cell0 + j;
+  EdgeState es[3];
+  bool sd;
+  float4 rk;
+  reconstruct(d, S->P, k, d.W0, es, sd, rk);
+  const int o = order[j];
+  const double z = d.z[k];
+  for (int i = 0; i < 3; i++) {
+    const double zz = z + (double)es[i].dz;
+    ze[3 * (size_t)o + i] = zz;
+    he[3 * (size_t)o + i] = es[i].h;
+    we[3 * (size_t)o + i] = zz + (double)es[i].h;
+    uhe[3 * (size_t)o + i] = es[i].uh;
+    vhe[3 * (size_t)o + i] = es[i].vh;
+  }
+}
+
+// update_timestep per scenario: one block reduces the scenario's tile
+// partials (minimum radius/speed as an FP64 key, boundary flux) and applies
+// the CFL/clamp logic.
+__global__ void k_pool_timestep(PoolDev d, int nscn) {
+  __shared__ float shf[TILE / 32];
+  __shared__ double shd[TILE / 32];
+  const int s = blockIdx.x;
+  if (s >= nscn) return;
+  PoolScn* S = d.scn + s;
+  if (!S->alive || !S->active) return;
+  float m = 3.0e38f;
+  double b = 0.0;
+  for (int t = S->tile0 + threadIdx.x; t < S->tile0 + S->ntile; t += blockDim.x) {
+    const float2 r = d.tile_red1[t];
+    m = fminf(m, r.x);
+    b += (double)r.y;
+  }
+  m = block_min_f(m, shf);
+  b = block_sum_d(b, shd);
+  if (threadIdx.x == 0) {
+    S->clock.dt_key = m < 3.0e38f ? ~(unsigned long long)__double_as_longlong((double)m) : 0ull;
+    S->clock.bfs_acc = b;
+    S->clock.bfs[0] = b;
+    timestep_logic(&S->clock);
+  }
+}
+
+__global__ void k_pool_reset(PoolDev d, int nscn) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nscn) return;
+  PoolScn* S = d.scn + s;
+  S->clock.dt_key = 0ull;
+  S->clock.bfs_acc = 0.0;
+}
+
+struct PoolOp {
+  int sid;
+  const int* idx;    // pool cells
+  int n;
+  double rate, factor;
+};
+
+__global__ void k_pool_rate(PoolDev d, PoolOp op, int slot) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  PoolScn* S = d.scn + op.sid;
+  if (!S->active || j >= op.n) return;
+  const int k = op.idx[j];
+  const double dt = S->clock.timestep;
+  double infl;
+  if (op.rate >= 0.0) {
+    const double local = op.factor * dt * op.rate;
+    d.wA[k] = d.wA[k] + local;
+    infl = local * d.area[k];
+  } else {
+    const double height = d.wA[k] - d.z[k];
+    const double local = fmax(op.factor * dt * op.rate, -height);
+    const double f = local < 0.0 ? (local + height) / (height + 1.0e-10) : 1.0;
+    d.wA[k] = d.wA[k] + local;
+    d.uhA[k] = d.uhA[k] * f;
+    d.vhA[k] = d.vhA[k] * f;
+    infl = local * d.area[k];
+  }
+  double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
+  d.W0[k] = protect_prep(S->P, w, uh, vh, d.z[k], d.area[k], added);
+  if (slot < MAX_OPS) atomicAdd(&S->clock.op_influx[slot], infl);
+}
+
+// Per-scenario clocks, one block each: stage-2 boundary flux reduction and
+// the end-of-step bookkeeping.  The last block to finish (ticket) sets the
+// graph's while condition when any scenario is still running.
+__global__ void k_pool_clock(PoolDev d, int nscn, cudaGraphConditionalHandle handle, int set_cond) {
+  __shared__ double shd[TILE / 32];
+  const int s = blockIdx.x;
+  PoolScn* S = d.scn + s;
+  const bool act = S->alive && S->active;
+  int running = 0;
+  if (act) {
+    double b = 0.0;
+    if (S->P.rk2)
+      for (int t = S->tile0 + threadIdx.x; t < S->tile0 + S->ntile; t += blockDim.x) b += (double)d.tile_red2[t];
+    b = block_sum_d(b, shd);
+    if (threadIdx.x == 0) {
+      S->clock.bfs[1] = b;
+      const int reason = clock_logic(&S->clock);
+      if (reason) S->active = 0;
+      else running = 1;
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (running) atomicAdd(&d.ctl[0], 1u);
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&d.ctl[1], 1u);
+    if (ticket == (unsigned int)nscn - 1u) {
+      __threadfence();
+      const unsigned int any = atomicAdd(&d.ctl[0], 0u);
+      d.ctl[0] = 0u;
+      d.ctl[1] = 0u;
+      __threadfence();
+      if (set_cond) cudaGraphSetConditional(handle, any ? 1u : 0u);
+    }
+  }
+}
+
+__global__ void k_gather(double* dst, const double* src, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[j] = src[order[j]];
+}
+__global__ void k_gather_f(float* dst, const double* src, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[j] = (float)src[order[j]];
+}
+__global__ void k_scatter(double* dst, const double* src, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[order[j]] = src[j];
+}
+__global__ void k_scatter_f(double* dst, const float* src, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[order[j]] = (double)src[j];
+}
+__global__ void k_scatter_height(double* dst, const double* w, const double* z, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[order[j]] = fmax(w[j] - z[j], 0.0);
+}
+__global__ void k_scatter_E(double* dst, const float4* E, int comp, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const float4 e = E[j];
+    dst[order[j]] = comp == 0 ? e.x : comp == 1 ? e.y : e.z;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+struct ScnHost {
+  int alive = 0;
+  int N = 0, B = 0, tile0 = 0, ntile = 0, bnd0 = 0, halo0 = 0, nhalo = 0;
+  agx_params prm{};
+  int* order = nullptr;          // device [N]: original index of each stored cell
+  double* series = nullptr;
+  std::vector<PoolOp> ops;
+  bool work_dirty = true;
+};
+
+struct Pool {
+  int device = 0;
+  int cap_cells = 0, cap_tiles = 0, cap_bnd = 0, cap_scn = 0, cap_halo = 0;
+  std::vector<int> halo_owner;   // host: halo slot owner (-1 free)
+  PoolDev d{};
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  int* tile_scn_dev = nullptr;
+  std::vector<int> tile_scn;     // host mirror
+  std::vector<int> bnd_owner;    // host: boundary slot owner (-1 free)
+  std::vector<ScnHost> scn;
+  PoolScn* scn_host = nullptr;   // pinned mirror of d.scn
+  double* staging = nullptr;     // device [cap_cells * 3] for permuted copies
+  double* staging_host = nullptr;
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_valid = false;
+  int grid = 0;
+  int kernels_per_iter = 0;
+  int mode_rk2_any = 1;
+};
+
+static thread_local char g_perr[512] = "";
+static agx_status pfail(agx_status c, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_perr, sizeof(g_perr), fmt, ap);
+  va_end(ap);
+  return c;
+}
+const char* pool_last_error() { return g_perr; }
+
+#define PCK(call)                                                                                     \
+  do {                                                                                                \
+    cudaError_t _e = (call);                                                                          \
+    if (_e != cudaSuccess) return pfail(AGX_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), \
+                                        __FILE__, __LINE__);                                          \
+  } while (0)
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t pool_layout(Pool* p, char* base) {
+  const size_t C = p->cap_cells, Bt = p->cap_bnd, T = p->cap_tiles, S = p->cap_scn;
+  size_t off = 0;
+  auto take = [&](size_t b) -> char* { char* r = base ? base + off : nullptr; off += al(b ? b : 8); return r; };
+  PoolDev& d = p->d;
+  d.conn = (const int4*)take(C * 16);
+  d.g0 = (const float4*)take(C * 16);
+  d.g1 = (const float4*)take(C * 16);
+  d.g2 = (const float4*)take(C * 16);
+  d.g3 = (float4*)take(C * 16);
+  d.g4 = (float4*)take(C * 16);
+  double** dd[] = {&d.wA, &d.uhA, &d.vhA, &d.wB, &d.uhB, &d.vhB, &d.z};
+  for (auto q : dd) *q = (double*)take(C * 8);
+  d.area = (const double*)take(C * 8);
+  d.eta = (float*)take(C * 4);
+  d.W0 = (float4*)take(C * 16);
+  d.W1 = (float4*)take(C * 16);
+  d.E = (float4*)take(C * 16);
+  d.maxs = (float*)take(C * 4);
+  d.bkind = (const int*)take(Bt * 4);
+  d.bval = (const double*)take(Bt * 24);
+  d.bcell = (const int*)take(Bt * 4);
+  d.lnk = (const int*)take(C * 4);
+  d.tile_halo = (const int2*)take(T * 8);
+  d.tile_red1 = (float2*)take(T * 8);
+  d.tile_red2 = (float*)take(T * 4);
+  d.ctl = (unsigned int*)take(64);
+  d.halo_cells = (const int*)take((size_t)p->cap_halo * 4);
+  p->tile_scn_dev = (int*)take(T * 4);
+  d.scn = (PoolScn*)take(S * sizeof(PoolScn));
+  p->staging = (double*)take(C * 8 * 5);
+  return off;
+}
+
+}  // namespace agx
+
+using namespace agx;
+
+struct agx_pool_s : public agx::Pool {};
+typedef agx_pool_s* agx_pool;
+
+static agx_status psync(Pool* p) {
+  PCK(cudaStreamSynchronize(p->stream));
+  return AGX_OK;
+}
+static agx_status pull_scn(Pool* p) {
+  PCK(cudaMemcpyAsync(p->scn_host, p->d.scn, sizeof(PoolScn) * p->cap_scn, cudaMemcpyDeviceToHost, p->stream));
+  return psync(p);
+}
+static agx_status push_scn(Pool* p) {
+  PCK(cudaMemcpyAsync(p->d.scn, p->scn_host, sizeof(PoolScn) * p->cap_scn, cudaMemcpyHostToDevice, p->stream));
+  return psync(p);
+}
+
+static MParams make_mparams(const agx_params& a) {
+  MParams P;
+  P.g = (float)a.g;
+  P.eps = (float)a.epsilon;
+  P.hmin = (float)a.minimum_allowed_height;
+  P.hmin64 = a.minimum_allowed_height;
+  P.beta_w = (float)a.beta_w;
+  P.beta_w_dry = (float)a.beta_w_dry;
+  P.beta_uh = (float)a.beta_uh;
+  P.beta_uh_dry = (float)a.beta_uh_dry;
+  P.beta_vh = (float)a.beta_vh;
+  P.beta_vh_dry = (float)a.beta_vh_dry;
+  const double c = 1.0 / (0.3 - 0.1);
+  P.c_tmp = (float)c;
+  P.d_tmp = (float)(1.0 - c * 0.3);
+  P.velocity_extrapolation = a.extrapolate_velocity_second_order == 1;
+  P.rk2 = a.timestepping_method == 2;
+  P.low_froude = a.low_froude;
+  P.pad = 0;
+  return P;
+}
+
+static void init_clock_p(Clock* c, const agx_params& p) {
+  memset(c, 0, sizeof(Clock));
+  c->final_time = -1.0;
+  c->yield_time = 1.0e300;
+  c->cfl = p.CFL;
+  c->max_dt = p.evolve_max_timestep;
+  c->min_dt = p.evolve_min_timestep;
+  c->recorded_min = p.evolve_max_timestep;
+  c->recorded_max = p.evolve_min_timestep;
+  c->max_smallsteps = p.max_smallsteps;
+  c->order = 2;
+  c->default_order = 2;
+  c->flux_timestep = p.evolve_max_timestep;
+}
+
+static int nblk1(int n) { return (n + 255) / 256; }
+
+static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  const PoolDev& d = p->d;
+  const int G = p->grid;
+  const int S = p->cap_scn;
+  k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
+  count_launch();
+  k_pool_flux<false><<<G, TILE, 0, st>>>(d);
+  count_launch();
+  phase_mark(st, PH_FLUX);
+  k_pool_timestep<<<S, TILE, 0, st>>>(d, S);
+  count_launch();
+  phase_mark(st, PH_SMALL);
+  // RK2 scenarios: update1 into B + flux2 fused; Euler scenarios only update.
+  // Both forms are handled by the same kernels with the per-scenario flag:
+  // the update kernel is launched once per form.
+  k_pool_update<<<std::max(d.ntiles, 1), TILE, 0, st>>>(d, 0);
+  count_launch();
+  phase_mark(st, PH_UPDATE);
+  k_pool_flux<true><<<G, TILE, 0, st>>>(d);
+  count_launch();
+  phase_mark(st, PH_FLUX);
+  for (size_t s = 0; s < p->scn.size(); s++) {
+    const ScnHost& sh = p->scn[s];
+    if (!sh.alive) continue;
+    for (size_t i = 0; i < sh.ops.size(); i++) {
+      const PoolOp& op = sh.ops[i];
+      k_pool_rate<<<nblk1(op.n), 256, 0, st>>>(d, op, (int)i);
+      count_launch();
+      phase_mark(st, PH_RATE);
+    }
+  }
+  k_pool_clock<<<S, TILE, 0, st>>>(d, S, (cudaGraphConditionalHandle)h, set_cond ? 1 : 0);
+  count_launch();
+  phase_mark(st, PH_SMALL);
+  return cudaGetLastError();
+}
+
+static agx_status pool_build_graph(Pool* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  PCK(cudaGraphCreate(&p->graph, 0));
+  cudaGraphConditionalHandle handle;
+  PCK(cudaGraphConditionalHandleCreate(&handle, p->graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = handle;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  PCK(cudaGraphAddNode(&node, p->graph, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  PCK(cudaStreamSynchronize(p->stream));
+  PCK(cudaStreamBeginCaptureToGraph(p->own_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  set_capturing(true);
+  cudaError_t e = enqueue_pool_iter(p, p->own_stream, (unsigned long long)handle, true);
+  set_capturing(false);
+  cudaGraph_t cap = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(p->own_stream, &cap);
+  if (e != cudaSuccess || e2 != cudaSuccess)
+    return pfail(AGX_E_CUDA, "pool capture failed: %s / %s", cudaGetErrorString(e), cudaGetErrorString(e2));
+  PCK(cudaGraphInstantiate(&p->exec, p->graph, 0));
+  size_t nn = 0;
+  PCK(cudaGraphGetNodes(body, nullptr, &nn));
+  p->kernels_per_iter = (int)nn;
+  p->graph_valid = true;
+  return AGX_OK;
+}
+
+extern "C" {
+
+agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_scenarios, agx_pool* out) {
+  if (!out || cap_cells <= 0 || cap_scenarios <= 0 || cap_boundary < 0)
+    return pfail(AGX_E_INVALID, "bad pool capacity");
+  *out = nullptr;
+  if (cap_cells > (1ll << 30)) return pfail(AGX_E_INVALID, "pool capacity above 2^30 cells");
+  agx_pool p = new agx_pool_s();
+  PCK(cudaGetDevice(&p->device));
+  p->cap_tiles = (int)((cap_cells + TILE - 1) / TILE) + cap_scenarios;
+  p->cap_cells = p->cap_tiles * TILE;
+  p->cap_bnd = (int)std::max<int64_t>(cap_boundary, 1);
+  p->cap_scn = cap_scenarios;
+  p->cap_halo = p->cap_cells / 2 + 1024;
+  const size_t bytes = pool_layout(p, nullptr);
+  cudaError_t e = cudaMalloc(&p->arena, bytes);
+  if (e != cudaSuccess) {
+    delete p;
+    return pfail(AGX_E_NOMEM, "pool allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  p->arena_bytes = bytes;
+  pool_layout(p, (char*)p->arena);
+  p->d.tile_scn = p->tile_scn_dev;
+  p->d.ntiles = 0;
+  p->tile_scn.assign(p->cap_tiles, -1);
+  p->bnd_owner.assign(p->cap_bnd, -1);
+  p->halo_owner.assign(p->cap_halo, -1);
+  p->scn.resize(p->cap_scn);
+  PCK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
+  p->stream = p->own_stream;
+  PCK(cudaMallocHost(&p->scn_host, sizeof(PoolScn) * p->cap_scn));
+  memset(p->scn_host, 0, sizeof(PoolScn) * p->cap_scn);
+  PCK(cudaMemsetAsync(p->arena, 0, bytes, p->stream));
+  PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, p->stream));
+  agx_status st = push_scn(p);
+  if (st) return st;
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false>, TILE, 0);
+  p->grid = std::max(1, sms * std::max(per, 1));
+  *out = p;
+  return AGX_OK;
+}
+
+int64_t agx_pool_footprint(int64_t cap_cells, int64_t cap_boundary, int32_t cap_scenarios) {
+  Pool tmp;
+  tmp.cap_tiles = (int)((cap_cells + TILE - 1) / TILE) + cap_scenarios;
+  tmp.cap_cells = tmp.cap_tiles * TILE;
+  tmp.cap_bnd = (int)std::max<int64_t>(cap_boundary, 1);
+  tmp.cap_scn = cap_scenarios;
+  tmp.cap_halo = tmp.cap_cells / 2 + 1024;
+  return (int64_t)pool_layout(&tmp, nullptr);
+}
+
+int64_t agx_pool_bytes_per_cell(void) {
+  // static tables + FP64 state (2 buffers) + work records + explicit update
+  return 16 * 6 + 8 * 8 + 4 + 16 * 3 + 4 + 8 * 5;
+}
+
+agx_status agx_pool_destroy(agx_pool p) {
+  if (!p) return AGX_OK;
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  for (auto& s : p->scn) {
+    if (s.order) cudaFree(s.order);
+    if (s.series) cudaFree(s.series);
+    for (auto& op : s.ops) if (op.idx) cudaFree((void*)op.idx);
+  }
+  if (p->arena) cudaFree(p->arena);
+  if (p->scn_host) cudaFreeHost(p->scn_host);
+  if (p->own_stream) cudaStreamDestroy(p->own_stream);
+  delete p;
+  return AGX_OK;
+}
+
+agx_status agx_pool_set_stream(agx_pool p, void* stream) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  agx_status st = psync(p);
+  if (st) return st;
+  p->stream = stream ? (cudaStream_t)stream : p->own_stream;
+  return AGX_OK;
+}
+
+// Add a scenario.  conn [N*4] (neighbours in the stored order, boundary
+// -(m+1), meta word), geo [N*16] floats (g0 g1 g2 g3 blocks: jump matrix,
+// edge vectors, radius; dz and inv_area are filled here), area [N],
+// order [N], boundary_cell [B] (stored order), lnk [N] (staging index of
+// each slot's neighbour), per tile halo_off/halo_cnt [ceil(N/TILE)] into
+// halo_cells [n_halo] (stored cell indices).
+agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, const float* geo,
+                        const double* area, const int32_t* order, const int32_t* bcell, const int32_t* lnk,
+                        const int32_t* halo_off, const int32_t* halo_cnt, int64_t n_halo,
+                        const int32_t* halo_cells, const agx_params* prm, int32_t* sid_out) {
+  if (!p || !conn || !geo || !area || !order || !prm || !sid_out || !lnk || !halo_off || !halo_cnt || N <= 0 ||
+      B < 0 || n_halo < 0)
+    return pfail(AGX_E_INVALID, "bad arguments");
+  if (prm->timestepping_method != 1 && prm->timestepping_method != 2)
+    return pfail(AGX_E_INVALID, "timestepping_method must be 1 or 2");
+  int sid = -1;
+  for (int s = 0; s < p->cap_scn; s++) if (!p->scn[s].alive) { sid = s; break; }
+  if (sid < 0) return pfail(AGX_E_NOMEM, "pool has no free scenario slot");
+  const int nt = (int)((N + TILE - 1) / TILE);
+  int t0 = -1;
+  for (int t = 0, run = 0; t < p->cap_tiles; t++) {
+    run = p->tile_scn[t] < 0 ? run + 1 : 0;
+    if (run == nt) { t0 = t - nt + 1; break; }
+  }
+  if (t0 < 0) return pfail(AGX_E_NOMEM, "pool has no %d free contiguous tiles", nt);
+  int b0 = 0;
+  if (B > 0) {
+    b0 = -1;
+    for (int b = 0, run = 0; b < p->cap_bnd; b++) {
+      run = p->bnd_owner[b] < 0 ? run + 1 : 0;
+      if (run == B) { b0 = b - (int)B + 1; break; }
+    }
+    if (b0 < 0) return pfail(AGX_E_NOMEM, "pool has no %lld free boundary slots", (long long)B);
+  }
+  int h0 = 0;
+  if (n_halo > 0) {
+    h0 = -1;
+    for (int h = 0, run = 0; h < p->cap_halo; h++) {
+      run = p->halo_owner[h] < 0 ? run + 1 : 0;
+      if (run == n_halo) { h0 = h - (int)n_halo + 1; break; }
+    }
+    if (h0 < 0) return pfail(AGX_E_NOMEM, "pool has no %lld free halo slots", (long long)n_halo);
+  }
+  for (int t = 0; t < nt; t++) {
+    if (halo_cnt[t] < 0 || halo_cnt[t] > HALO_MAX || halo_off[t] < 0 || halo_off[t] + halo_cnt[t] > n_halo)
+      return pfail(AGX_E_INVALID, "bad halo table at tile %d", t);
+  }
+  for (int64_t k = 0; k < N; k++) {
+    for (int i = 0; i < 3; i++) {
+      const int li = (lnk[k] >> (10 * i)) & 1023;
+      if (li != LNK_INLINE && li >= TILE + halo_cnt[k / TILE])
+        return pfail(AGX_E_INVALID, "bad staging index at cell %lld", (long long)k);
+    }
+  }
+  const int c0 = t0 * TILE;
+  // relocate indices to the pool
+  std::vector<int32_t> cc((size_t)N * 4);
+  for (int64_t k = 0; k < N; k++) {
+    for (int i = 0; i < 3; i++) {
+      const int32_t n = conn[4 * k + i];
+      if (n >= 0) {
+        if (n >= N) return pfail(AGX_E_INVALID, "neighbour index out of range");
+        cc[4 * k + i] = n + c0;
+      } else {
+        const int32_t m = -n - 1;
+        if (m >= B) return pfail(AGX_E_INVALID, "boundary index out of range");
+        cc[4 * k + i] = -(m + b0) - 1;
+      }
+    }
+    cc[4 * k + 3] = conn[4 * k + 3];
+  }
+  std::vector<float> G[5];
+  for (int g = 0; g < 5; g++) G[g].assign((size_t)N * 4, 0.f);
+  for (int64_t k = 0; k < N; k++)
+    for (int g = 0; g < 4; g++)
+      for (int c = 0; c < 4; c++) G[g][4 * k + c] = geo[16 * k + 4 * g + c];
+  for (int64_t k = 0; k < N; k++) G[4][4 * k + 3] = (float)(1.0 / area[k]);
+  cudaStream_t st = p->stream;
+  PCK(cudaMemcpyAsync((void*)(p->d.conn + c0), cc.data(), N * 16, cudaMemcpyHostToDevice, st));
+  const float4* gd[5] = {p->d.g0, p->d.g1, p->d.g2, p->d.g3, p->d.g4};
+  for (int g = 0; g < 5; g++) PCK(cudaMemcpyAsync((void*)(gd[g] + c0), G[g].data(), N * 16, cudaMemcpyHostToDevice, st));
+  PCK(cudaMemcpyAsync((void*)(p->d.area + c0), area, N * 8, cudaMemcpyHostToDevice, st));
+  PCK(cudaMemcpyAsync((void*)(p->d.lnk + c0), lnk, N * 4, cudaMemcpyHostToDevice, st));
+  {
+    std::vector<int2> th(nt);
+    for (int t = 0; t < nt; t++) th[t] = make_int2(halo_off[t] + h0, halo_cnt[t]);
+    PCK(cudaMemcpyAsync((void*)(p->d.tile_halo + t0), th.data(), nt * 8, cudaMemcpyHostToDevice, st));
+    if (n_halo > 0) {
+      std::vector<int32_t> hc(n_halo);
+      for (int64_t h = 0; h < n_halo; h++) {
+        if (halo_cells[h] < 0 || halo_cells[h] >= N) return pfail(AGX_E_INVALID, "halo cell out of range");
+        hc[h] = halo_cells[h] + c0;
+      }
+      PCK(cudaMemcpyAsync((void*)(p->d.halo_cells + h0), hc.data(), n_halo * 4, cudaMemcpyHostToDevice, st));
+      PCK(cudaStreamSynchronize(st));
+    }
+  }
+  ScnHost& sh = p->scn[sid];
+  sh = ScnHost();
+  PCK(cudaMalloc(&sh.order, N * 4));
+  PCK(cudaMemcpyAsync(sh.order, order, N * 4, cudaMemcpyHostToDevice, st));
+  if (B > 0) {
+    std::vector<int32_t> bc(B);
+    for (int64_t m = 0; m < B; m++) bc[m] = bcell[m] + c0;
+    PCK(cudaMemcpyAsync((void*)(p->d.bcell + b0), bc.data(), B * 4, cudaMemcpyHostToDevice, st));
+    PCK(cudaMemsetAsync((void*)(p->d.bkind + b0), 0, B * 4, st));
+    PCK(cudaMemsetAsync((void*)(p->d.bval + 3 * (size_t)b0), 0, B * 24, st));
+  }
+  // zero the scenario's dynamic arrays
+  double* zd[] = {p->d.wA, p->d.uhA, p->d.vhA, p->d.wB, p->d.uhB, p->d.vhB, p->d.z};
+  for (double* a : zd) PCK(cudaMemsetAsync(a + c0, 0, (size_t)nt * TILE * 8, st));
+  PCK(cudaMemsetAsync(p->d.eta + c0, 0, (size_t)nt * TILE * 4, st));
+  PCK(cudaMemsetAsync(p->d.W0 + c0, 0, (size_t)nt * TILE * 16, st));
+  PCK(cudaMemsetAsync(p->d.W1 + c0, 0, (size_t)nt * TILE * 16, st));
+  PCK(cudaMemsetAsync(p->d.E + c0, 0, (size_t)nt * TILE * 16, st));
+  PCK(cudaMemsetAsync(p->d.maxs + c0, 0, (size_t)nt * TILE * 4, st));
+  for (int t = t0; t < t0 + nt; t++) p->tile_scn[t] = sid;
+  for (int b = b0; b < b0 + B; b++) p->bnd_owner[b] = sid;
+  for (int h = h0; h < h0 + n_halo; h++) p->halo_owner[h] = sid;
+  int ntiles = 0;
+  for (int t = 0; t < p->cap_tiles; t++) if (p->tile_scn[t] >= 0) ntiles = t + 1;
+  PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, st));
+  agx_status s2 = pull_scn(p);
+  if (s2) return s2;
+  PoolScn& S = p->scn_host[sid];
+  memset(&S, 0, sizeof(S));
+  init_clock_p(&S.clock, *prm);
+  S.P = make_mparams(*prm);
+  S.cell0 = c0;
+  S.ncell = (int)N;
+  S.tile0 = t0;
+  S.ntile = nt;
+  S.bnd0 = b0;
+  S.nbnd = (int)B;
+  S.alive = 1;
+  S.active = 0;
+  if ((s2 = push_scn(p))) return s2;
+  sh.alive = 1;
+  sh.N = (int)N;
+  sh.B = (int)B;
+  sh.tile0 = t0;
+  sh.ntile = nt;
+  sh.bnd0 = b0;
+  sh.halo0 = h0;
+  sh.nhalo = (int)n_halo;
+  sh.prm = *prm;
+  sh.work_dirty = true;
+  if (ntiles != p->d.ntiles) {
+    p->d.ntiles = ntiles;
+    p->graph_valid = false;
+  }
+  *sid_out = sid;
+  return AGX_OK;
+}
+
+agx_status agx_pool_remove(agx_pool p, int32_t sid) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  ScnHost& sh = p->scn[sid];
+  for (int t = sh.tile0; t < sh.tile0 + sh.ntile; t++) p->tile_scn[t] = -1;
+  for (int b = sh.bnd0; b < sh.bnd0 + sh.B; b++) p->bnd_owner[b] = -1;
+  for (int h = sh.halo0; h < sh.halo0 + sh.nhalo; h++) p->halo_owner[h] = -1;
+  PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, p->stream));
+  p->scn_host[sid].alive = 0;
+  p->scn_host[sid].active = 0;
+  if ((st = push_scn(p))) return st;
+  if (sh.order) cudaFree(sh.order);
+  if (sh.series) cudaFree(sh.series);
+  bool had_ops = !sh.ops.empty();
+  for (auto& op : sh.ops) if (op.idx) cudaFree((void*)op.idx);
+  sh = ScnHost();
+  int ntiles = 0;
+  for (int t = 0; t < p->cap_tiles; t++) if (p->tile_scn[t] >= 0) ntiles = t + 1;
+  if (ntiles != p->d.ntiles || had_ops) {
+    p->d.ntiles = ntiles;
+    p->graph_valid = false;
+  }
+  return AGX_OK;
+}
+
+static agx_status ensure_work(Pool* p, int sid) {
+  ScnHost& sh = p->scn[sid];
+  if (!sh.work_dirty) return AGX_OK;
+  k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 0, sid);
+  count_launch();
+  PCK(cudaGetLastError());
+  sh.work_dirty = false;
+  return psync(p);
+}
+
+// Field access in the caller's (original) cell order.
+agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t f, const double* host, int64_t n) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (n != sh.N) return pfail(AGX_E_INVALID, "field needs %d values", sh.N);
+  const int c0 = sh.tile0 * TILE;
+  double* dst = nullptr;
+  switch (f) {
+    case AGX_STAGE_C: dst = p->d.wA; break;
+    case AGX_XMOM_C: dst = p->d.uhA; break;
+    case AGX_YMOM_C: dst = p->d.vhA; break;
+    case AGX_ELEV_C: dst = p->d.z; break;
+    case AGX_FRICTION_C: break;
+    default: return pfail(AGX_E_STATE, "field %d cannot be set on a mixed-precision scenario", f);
+  }
+  PCK(cudaMemcpyAsync(p->staging, host, n * 8, cudaMemcpyHostToDevice, p->stream));
+  if (f == AGX_FRICTION_C) {
+    k_gather_f<<<nblk1((int)n), 256, 0, p->stream>>>(p->d.eta + c0, p->staging, sh.order, (int)n);
+  } else {
+    k_gather<<<nblk1((int)n), 256, 0, p->stream>>>(dst + c0, p->staging, sh.order, (int)n);
+  }
+  count_launch();
+  if (f == AGX_ELEV_C) {
+    k_pool_dz<<<p->grid, TILE, 0, p->stream>>>(p->d, sid);
+    count_launch();
+  }
+  PCK(cudaGetLastError());
+  sh.work_dirty = true;
+  return psync(p);
+}
+
+agx_status agx_pool_get_field(agx_pool p, int32_t sid, int32_t f, double* host, int64_t n) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  const int N = sh.N;
+  const int c0 = sh.tile0 * TILE;
+  const bool edge = f >= AGX_STAGE_E && f <= AGX_HEIGHT_V;
+  if (n != (edge ? 3 * (int64_t)N : N)) return pfail(AGX_E_INVALID, "field size mismatch");
+  double* out = p->staging;
+  cudaStream_t st = p->stream;
+  switch (f) {
+    case AGX_STAGE_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, sh.order, N); break;
+    case AGX_XMOM_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.uhA + c0, sh.order, N); break;
+    case AGX_YMOM_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.vhA + c0, sh.order, N); break;
+    case AGX_ELEV_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.z + c0, sh.order, N); break;
+    case AGX_FRICTION_C: k_scatter_f<<<nblk1(N), 256, 0, st>>>(out, p->d.eta + c0, sh.order, N); break;
+    case AGX_HEIGHT_C: k_scatter_height<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, p->d.z + c0, sh.order, N); break;
+    case AGX_MAX_SPEED: k_scatter_f<<<nblk1(N), 256, 0, st>>>(out, p->d.maxs + c0, sh.order, N); break;
+    case AGX_STAGE_X: case AGX_XMOM_X: case AGX_YMOM_X:
+      k_scatter_E<<<nblk1(N), 256, 0, st>>>(out, p->d.E + c0, f - AGX_STAGE_X, sh.order, N); break;
+    default:
+      if (edge) {
+        agx_status s2 = ensure_work(p, sid);
+        if (s2) return s2;
+        double* tmp = nullptr;
+        PCK(cudaMalloc(&tmp, (size_t)15 * N * 8));
+        double* we = tmp;
+        double* he = we + 3 * (size_t)N;
+        double* uhe = he + 3 * (size_t)N;
+        double* vhe = uhe + 3 * (size_t)N;
+        double* ze = vhe + 3 * (size_t)N;
+        k_pool_edges<<<nblk1(N), 256, 0, st>>>(p->d, sid, we, he, uhe, vhe, ze, sh.order);
+        count_launch();
+        const int idx = (f - AGX_STAGE_E) % 5;     // stage, xmom, ymom, elev, height
+        double* src[5] = {we, uhe, vhe, ze, he};
+        cudaError_t ce = cudaMemcpyAsync(host, src[idx], 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, st);
+        agx_status s3 = psync(p);
+        cudaFree(tmp);
+        if (ce != cudaSuccess) return pfail(AGX_E_CUDA, "edge export copy failed: %s", cudaGetErrorString(ce));
+        if (s3) return s3;
+        if (f >= AGX_STAGE_V) {
+          // vertex values from edge values on the host
+          for (int64_t k = 0; k < N; k++) {
+            const double e0 = host[3 * k], e1 = host[3 * k + 1], e2 = host[3 * k + 2];
+            host[3 * k] = e1 + e2 - e0;
+            host[3 * k + 1] = e0 + e2 - e1;
+            host[3 * k + 2] = e0 + e1 - e2;
+          }
+        }
+        return AGX_OK;
+      }
+      return pfail(AGX_E_STATE, "field %d is not kept by the mixed-precision scenario", f);
+  }
+  count_launch();
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(host, out, n * 8, cudaMemcpyDeviceToHost, st));
+  return psync(p);
+}
+
+agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, const double* values, int64_t B) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (B != sh.B) return pfail(AGX_E_INVALID, "boundary arrays need %d entries", sh.B);
+  if (B == 0) return AGX_OK;
+  PCK(cudaMemcpyAsync((void*)(p->d.bkind + sh.bnd0), kind, B * 4, cudaMemcpyHostToDevice, p->stream));
+  if (values) PCK(cudaMemcpyAsync((void*)(p->d.bval + 3 * (size_t)sh.bnd0), values, B * 24, cudaMemcpyHostToDevice, p->stream));
+  return psync(p);
+}
+
+agx_status agx_pool_set_boundary_series(agx_pool p, int32_t sid, const double* rows, int64_t n) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || n < 0) return pfail(AGX_E_INVALID, "bad arguments");
+  ScnHost& sh = p->scn[sid];
+  agx_status st = psync(p);
+  if (st) return st;
+  if (sh.series) cudaFree(sh.series);
+  sh.series = nullptr;
+  if (n > 0) {
+    PCK(cudaMalloc(&sh.series, n * 32));
+    PCK(cudaMemcpyAsync(sh.series, rows, n * 32, cudaMemcpyHostToDevice, p->stream));
+  }
+  if ((st = pull_scn(p))) return st;
+  p->scn_host[sid].series = sh.series;
+  p->scn_host[sid].nseries = (int)n;
+  return push_scn(p);
+}
+
+agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double rate, double factor) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (sh.ops.size() >= (size_t)MAX_OPS) return pfail(AGX_E_INVALID, "at most %d operators", MAX_OPS);
+  // indices are in the caller's order: map them to pool cells on the host
+  std::vector<int32_t> ord(sh.N);
+  PCK(cudaMemcpyAsync(ord.data(), sh.order, sh.N * 4, cudaMemcpyDeviceToHost, p->stream));
+  agx_status st = psync(p);
+  if (st) return st;
+  std::vector<int32_t> inv(sh.N);
+  for (int j = 0; j < sh.N; j++) inv[ord[j]] = j;
+  std::vector<int32_t> cells;
+  const int c0 = sh.tile0 * TILE;
+  if (idx) {
+    for (int64_t i = 0; i < n; i++) {
+      if (idx[i] < 0 || idx[i] >= sh.N) return pfail(AGX_E_INVALID, "operator index out of range");
+      cells.push_back(inv[idx[i]] + c0);
+    }
+  } else {
+    for (int j = 0; j < sh.N; j++) cells.push_back(c0 + j);
+  }
+  PoolOp op{sid, nullptr, (int)cells.size(), rate, factor};
+  if (!cells.empty()) {
+    int* dptr = nullptr;
+    PCK(cudaMalloc(&dptr, cells.size() * 4));
+    PCK(cudaMemcpyAsync(dptr, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice, p->stream));
+    op.idx = dptr;
+  }
+  sh.ops.push_back(op);
+  p->graph_valid = false;
+  return psync(p);
+}
+
+agx_status agx_pool_clear_operators(agx_pool p, int32_t sid) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  agx_status st = psync(p);
+  if (st) return st;
+  for (auto& op : p->scn[sid].ops) if (op.idx) cudaFree((void*)op.idx);
+  p->scn[sid].ops.clear();
+  p->graph_valid = false;
+  return AGX_OK;
+}
+
+// distribute_to_vertices_and_edges for one scenario (protect in place,
+// surrounded-dry zeroing, fresh work record).
+agx_status agx_pool_distribute(agx_pool p, int32_t sid) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 1, sid);
+  k_pool_sdry<<<p->grid, TILE, 0, p->stream>>>(p->d, sid);
+  k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 0, sid);
+  count_launch(3);
+  PCK(cudaGetLastError());
+  p->scn[sid].work_dirty = false;
+  return psync(p);
+}
+
+agx_status agx_pool_set_clock(agx_pool p, int32_t sid, double time, double yield_time, double final_time,
+                              int64_t max_steps) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  Clock& c = p->scn_host[sid].clock;
+  c.time = time;
+  c.yield_time = yield_time;
+  c.final_time = final_time;
+  c.steps_target = max_steps > 0 ? max_steps : 0;
+  c.steps_call = 0;
+  c.reason = 0;
+  c.recorded_min = p->scn[sid].prm.evolve_max_timestep;
+  c.recorded_max = p->scn[sid].prm.evolve_min_timestep;
+  p->scn_host[sid].active = 1;
+  return push_scn(p);
+}
+
+agx_status agx_pool_deactivate(agx_pool p, int32_t sid) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  p->scn_host[sid].active = 0;
+  return push_scn(p);
+}
+
+static void fill_stats_p(const Clock* c, agx_step_stats* o) {
+  o->time = c->time;
+  o->last_timestep = c->timestep;
+  o->min_timestep = c->recorded_min;
+  o->max_timestep = c->recorded_max;
+  o->flux_timestep = c->flux_timestep;
+  o->mass_added = c->mass_added;
+  for (int i = 0; i < 3; i++) o->boundary_flux_sum[i] = c->bfs[i];
+  o->steps = c->steps_call;
+  o->total_steps = c->total_steps;
+  o->negative_cells = c->negative_cells;
+  o->reason = c->reason;
+  o->order = c->order;
+}
+
+// Advance every active scenario until each reaches its yield time, final
+// time or step target.  One graph launch (device-side while loop).
+agx_status agx_pool_advance(agx_pool p, int32_t* n_done) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  int nact = 0;
+  for (int s = 0; s < p->cap_scn; s++) if (p->scn_host[s].alive && p->scn_host[s].active) nact++;
+  if (nact == 0) { if (n_done) *n_done = 0; return AGX_OK; }
+  if (!p->graph_valid && (st = pool_build_graph(p)) != AGX_OK) return st;
+  PCK(cudaGraphLaunch(p->exec, p->stream));
+  if ((st = pull_scn(p))) return st;
+  long long iters = 0;
+  int done = 0;
+  for (int s = 0; s < p->cap_scn; s++) {
+    if (!p->scn_host[s].alive) continue;
+    iters = std::max(iters, p->scn_host[s].clock.steps_call);
+    if (p->scn_host[s].clock.reason) done++;
+  }
+  count_launch(iters * p->kernels_per_iter);
+  if (n_done) *n_done = done;
+  return AGX_OK;
+}
+
+agx_status agx_pool_get_stats(agx_pool p, int32_t sid, agx_step_stats* out) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !out) return pfail(AGX_E_INVALID, "bad scenario");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  fill_stats_p(&p->scn_host[sid].clock, out);
+  const int e = p->scn_host[sid].clock.error;
+  if (e & ERR_NUMERIC) return pfail(AGX_E_NUMERIC, "non-positive semi-implicit denominator");
+  if (e & ERR_TIMESTEP) return pfail(AGX_E_TIMESTEP, "too small timestep at first order");
+  if (e & ERR_NAN) return pfail(AGX_E_NUMERIC, "non-finite or non-positive timestep (state diverged)");
+  if (e & ERR_OVERSHOOT) return pfail(AGX_E_OVERSHOOT, "time overshot finaltime");
+  if (e & ERR_STEPCAP) return pfail(AGX_E_STATE, "device loop hit the per-call step cap");
+  return AGX_OK;
+}
+
+agx_status agx_pool_operator_influx(agx_pool p, int32_t sid, int32_t op, double* v) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || op < 0 || op >= MAX_OPS || !v)
+    return pfail(AGX_E_INVALID, "bad arguments");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  *v = p->scn_host[sid].clock.op_influx[op];
+  return AGX_OK;
+}
+
+// Per-kernel event timing of `reps` iterations (direct launches).
+agx_status agx_pool_time_phases(agx_pool p, int32_t reps, double* ms, int32_t n_cat) {
+  if (!p || !ms || reps <= 0 || n_cat < PH_COUNT) return pfail(AGX_E_INVALID, "bad arguments");
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
+  agx_status st0 = pull_scn(p);
+  if (st0) return st0;
+  std::vector<PoolScn> saved(p->scn_host, p->scn_host + p->cap_scn);
+  for (int s = 0; s < p->cap_scn; s++) {
+    if (!p->scn_host[s].alive) continue;
+    p->scn_host[s].active = 1;
+    p->scn_host[s].clock.yield_time = 1.0e300;
+    p->scn_host[s].clock.final_time = -1.0;
+    p->scn_host[s].clock.steps_target = 0;
+  }
+  if ((st0 = push_scn(p))) return st0;
+  for (int i = 0; i < n_cat; i++) ms[i] = 0.0;
+  cudaEvent_t start;
+  cudaEventCreate(&start);
+  for (int r = 0; r < reps; r++) {
+    begin_phase_timer();
+    cudaEventRecord(start, p->stream);
+    cudaError_t e = enqueue_pool_iter(p, p->stream, 0ull, false);
+    if (e != cudaSuccess) { end_phase_timer(nullptr, 0, start, 1); return pfail(AGX_E_CUDA, "%s", cudaGetErrorString(e)); }
+    PCK(cudaStreamSynchronize(p->stream));
+    end_phase_timer(ms, reps, start, 0);
+  }
+  cudaEventDestroy(start);
+  // restore activity and the clock targets (the state itself has advanced)
+  if ((st0 = pull_scn(p))) return st0;
+  for (int s = 0; s < p->cap_scn; s++) {
+    if (!p->scn_host[s].alive) continue;
+    p->scn_host[s].active = saved[s].active;
+    p->scn_host[s].clock.yield_time = saved[s].clock.yield_time;
+    p->scn_host[s].clock.final_time = saved[s].clock.final_time;
+    p->scn_host[s].clock.steps_target = saved[s].clock.steps_target;
+  }
+  return push_scn(p);
+}
+
+int32_t agx_pool_grid(agx_pool p) { return p ? p->grid : 0; }
+
+int32_t agx_pool_last_error(char* buf, int32_t n) {
+  if (buf && n > 0) {
+    strncpy(buf, g_perr, (size_t)n - 1);
+    buf[n - 1] = 0;
+  }
+  return (int32_t)strlen(g_perr);
+}
+
+}  // extern "C"

@@ -235,36 +235,10 @@ __global__ void k_accum(Dev d, int substep) {
   }
 }
 
-// update_timestep (generic_domain.py:2349-2415) and the flux_timestep
-// bookkeeping of compute_fluxes; one thread.
 __global__ void k_timestep(Dev d, int substep_count) {
-  Clock* c = d.clock;
-  const unsigned long long key = c->dt_key;
-  const double flux_dt = key ? __longlong_as_double((long long)~key) : 1.0e100;
-  c->flux_timestep = flux_dt;
-  c->bfs[0] = c->bfs_acc;
-  double ts = fmin(c->cfl * flux_dt, c->max_dt);
-  c->recorded_max = fmax(ts, c->recorded_max);
-  c->recorded_min = fmin(ts, c->recorded_min);
-  if (ts < c->min_dt) {
-    c->smallsteps += 1;
-    if (c->smallsteps > c->max_smallsteps) {
-      c->smallsteps = 0;
-      if (c->order == 1) {
-        c->error |= ERR_TIMESTEP;
-        ts = c->min_dt;
-      } else {
-        c->order = 1;
-      }
-    }
-  } else {
-    c->smallsteps = 0;
-    if (c->order == 1 && c->default_order == 2) c->order = 2;
-  }
-  if (c->final_time >= 0.0 && c->time + ts > c->final_time) ts = c->final_time - c->time;
-  if (c->time + ts > c->yield_time) ts = c->yield_time - c->time;
-  c->timestep = ts;
   (void)substep_count;
+  d.clock->bfs[0] = d.clock->bfs_acc;
+  timestep_logic(d.clock);
 }
 
 __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int saxpy) {
@@ -367,34 +341,9 @@ __global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor,
   }
 }
 
-// End of one step (generic_domain.py:1851-1912): advance time, count, and
-// decide whether the device loop continues.
 __global__ void k_clock(Dev d, double t0_unused, cudaGraphConditionalHandle handle, int set_cond) {
-  Clock* c = d.clock;
   (void)t0_unused;
-  c->time = c->time + c->timestep;
-  c->steps_call += 1;
-  c->total_steps += 1;
-  int reason = 0;
-  // Guards that keep the device loop finite: a NaN time or timestep, a
-  // non-positive timestep, or the per-call step cap end the loop with an error.
-  if (!(c->time == c->time) || !(c->timestep == c->timestep)) c->error |= ERR_NAN;
-  if (!(c->timestep > 0.0) && !(c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) &&
-      !(c->time >= c->yield_time))
-    c->error |= ERR_NAN;
-  if (c->steps_call >= MAX_STEPS_PER_CALL) c->error |= ERR_STEPCAP;
-  if (c->error) {
-    reason = AGX_STOP_ERROR;
-  } else if (c->steps_target > 0 && c->steps_call >= c->steps_target) {
-    reason = AGX_STOP_MAXSTEPS;
-  } else if (c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) {
-    if (c->time > c->final_time) c->error |= ERR_OVERSHOOT;
-    c->time = c->final_time;
-    reason = AGX_STOP_FINAL;
-  } else if (c->time >= c->yield_time) {
-    reason = AGX_STOP_YIELD;
-  }
-  c->reason = reason;
+  const int reason = clock_logic(d.clock);
   if (set_cond) cudaGraphSetConditional(handle, reason == 0 ? 1u : 0u);
 }
 

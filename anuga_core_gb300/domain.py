@@ -389,13 +389,13 @@ class Domain:
         per_side = None
         if self.low_froude:
             per_side = np.ones((len(self), 3), bool)
-        if not hasattr(self, "_tables") or self._tables_key != (self.low_froude,):
-            self._tables = pack_tables(self.mesh, per_side_edges=per_side)
-            self._tables_key = (self.low_froude,)
         if self.precision == "mixed":
             from .mixed import MixedScenario
-            self._scn = MixedScenario(self.mesh, self._tables, self._params())
+            self._scn = MixedScenario(self.mesh, None, self._params())
         else:
+            if not hasattr(self, "_tables") or self._tables_key != (self.low_froude,):
+                self._tables = pack_tables(self.mesh, per_side_edges=per_side)
+                self._tables_key = (self.low_froude,)
             self._scn = _lib.Scenario(self._tables, self._params())
         up = self._upload_fields()
         for f in self._fstate:
@@ -407,6 +407,8 @@ class Domain:
         return self._scn
 
     def _upload_fields(self):
+        if self.precision == "mixed":
+            return {"stage_c", "xmom_c", "ymom_c", "elev_c", "friction_c"}
         return {"stage_c", "xmom_c", "ymom_c", "elev_c", "friction_c", "elev_v",
                 "stage_e", "xmom_e", "ymom_e", "elev_e", "height_e",
                 "stage_b", "xmom_b", "ymom_b", "stage_s", "xmom_s", "ymom_s"}

@@ -1,0 +1,287 @@
+"""Mixed-precision scenarios on a device pool (ctypes binding of agx_pool_*).
+
+``Pool`` holds many scenarios in one device arena and advances every active
+one per graph launch (the batched and serving forms).  ``MixedScenario`` is a
+pool with one scenario, exposing the interface the Domain uses for the plain
+FP64 scenario, so ``Domain.set_gpu_options(precision='mixed')`` switches the
+step to the mixed-precision kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .tables import pack_mixed
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_pool_lib = None
+
+
+def lib():
+    global _pool_lib
+    if _pool_lib is None:
+        L = _lib.load()
+        H = ctypes.c_void_p
+        P = ctypes.POINTER
+        sig = {
+            "agx_pool_create": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, P(H)], ctypes.c_int32),
+            "agx_pool_destroy": ([H], ctypes.c_int32),
+            "agx_pool_footprint": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32], ctypes.c_int64),
+            "agx_pool_bytes_per_cell": ([], ctypes.c_int64),
+            "agx_pool_set_stream": ([H, ctypes.c_void_p], ctypes.c_int32),
+            "agx_pool_add": ([H, ctypes.c_int64, ctypes.c_int64, _i32p, _f32p, _f64p, _i32p, _i32p, _i32p,
+                              _i32p, _i32p, ctypes.c_int64, _i32p, P(_lib.Params), P(ctypes.c_int32)],
+                             ctypes.c_int32),
+            "agx_pool_remove": ([H, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_set_field": ([H, ctypes.c_int32, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_get_field": ([H, ctypes.c_int32, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_set_boundary": ([H, ctypes.c_int32, _i32p, _f64p, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_set_boundary_series": ([H, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_add_rate": ([H, ctypes.c_int32, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double],
+                                  ctypes.c_int32),
+            "agx_pool_clear_operators": ([H, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_set_clock": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_deactivate": ([H, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_advance": ([H, P(ctypes.c_int32)], ctypes.c_int32),
+            "agx_pool_get_stats": ([H, ctypes.c_int32, P(_lib.StepStats)], ctypes.c_int32),
+            "agx_pool_operator_influx": ([H, ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
+            "agx_pool_time_phases": ([H, ctypes.c_int32, _f64p, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_grid": ([H], ctypes.c_int32),
+            "agx_pool_last_error": ([ctypes.c_char_p, ctypes.c_int32], ctypes.c_int32),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _pool_lib = L
+    return _pool_lib
+
+
+def _err():
+    buf = ctypes.create_string_buffer(512)
+    lib().agx_pool_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def check(code):
+    if code != 0:
+        raise _lib.AgxError(code, _err())
+    return code
+
+
+def footprint(cells, boundary, scenarios=1):
+    return int(lib().agx_pool_footprint(int(cells), int(boundary), int(scenarios)))
+
+
+def bytes_per_cell():
+    return int(lib().agx_pool_bytes_per_cell())
+
+
+class Pool:
+    """Device pool of mixed-precision scenarios (capacities fixed at creation)."""
+
+    def __init__(self, cap_cells, cap_boundary, cap_scenarios=1):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        check(self.L.agx_pool_create(int(cap_cells), int(cap_boundary), int(cap_scenarios), ctypes.byref(h)))
+        self.h = h
+        self.cap_cells = int(cap_cells)
+        self.cap_boundary = int(cap_boundary)
+        self.cap_scenarios = int(cap_scenarios)
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.agx_pool_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, ptr):
+        check(self.L.agx_pool_set_stream(self.h, ctypes.c_void_p(ptr or 0)))
+
+    def add(self, mesh, params, tables=None):
+        T = tables if tables is not None else pack_mixed(mesh)
+        N = T["conn"].shape[0]
+        B = T["boundary_cell"].shape[0]
+        sid = ctypes.c_int32()
+        hc = T["halo_cells"] if T["halo_cells"].size else np.zeros(1, np.int32)
+        check(self.L.agx_pool_add(self.h, N, B, T["conn"].ctypes.data_as(_i32p), T["geo"].ctypes.data_as(_f32p),
+                                  T["area"].ctypes.data_as(_f64p), T["order"].ctypes.data_as(_i32p),
+                                  T["boundary_cell"].ctypes.data_as(_i32p), T["lnk"].ctypes.data_as(_i32p),
+                                  T["halo_off"].ctypes.data_as(_i32p), T["halo_cnt"].ctypes.data_as(_i32p),
+                                  T["halo_cells"].size, hc.ctypes.data_as(_i32p), ctypes.byref(params),
+                                  ctypes.byref(sid)))
+        self._keep[sid.value] = (N, B)
+        return sid.value
+
+    def remove(self, sid):
+        check(self.L.agx_pool_remove(self.h, int(sid)))
+        self._keep.pop(sid, None)
+
+    def set_field(self, sid, name, values):
+        a = np.ascontiguousarray(np.asarray(values, np.float64).ravel())
+        check(self.L.agx_pool_set_field(self.h, sid, _lib.FIELD[name], a.ctypes.data_as(_f64p), a.size))
+
+    def get_field(self, sid, name, out=None):
+        N, _ = self._keep[sid]
+        n = 3 * N if (name.endswith("_e") or name.endswith("_v")) else N
+        a = np.empty(n, np.float64) if out is None else out
+        check(self.L.agx_pool_get_field(self.h, sid, _lib.FIELD[name], a.ctypes.data_as(_f64p), n))
+        return a
+
+    def set_boundary(self, sid, kind, values):
+        k = np.ascontiguousarray(kind, np.int32)
+        v = np.ascontiguousarray(values, np.float64).reshape(-1)
+        check(self.L.agx_pool_set_boundary(self.h, sid, k.ctypes.data_as(_i32p), v.ctypes.data_as(_f64p), k.size))
+
+    def set_boundary_series(self, sid, rows):
+        r = np.ascontiguousarray(rows, np.float64).reshape(-1, 4)
+        check(self.L.agx_pool_set_boundary_series(self.h, sid, r.ctypes.data_as(_f64p), r.shape[0]))
+
+    def add_rate(self, sid, indices, rate, factor=1.0):
+        if indices is None:
+            check(self.L.agx_pool_add_rate(self.h, sid, None, 0, float(rate), float(factor)))
+        else:
+            idx = np.ascontiguousarray(indices, np.int32)
+            check(self.L.agx_pool_add_rate(self.h, sid, idx.ctypes.data_as(_i32p), idx.size, float(rate),
+                                           float(factor)))
+
+    def clear_operators(self, sid):
+        check(self.L.agx_pool_clear_operators(self.h, sid))
+
+    def operator_influx(self, sid, op):
+        v = ctypes.c_double()
+        check(self.L.agx_pool_operator_influx(self.h, sid, op, ctypes.byref(v)))
+        return v.value
+
+    def distribute(self, sid):
+        check(self.L.agx_pool_distribute(self.h, sid))
+
+    def set_clock(self, sid, time, yield_time, final_time, max_steps=0):
+        check(self.L.agx_pool_set_clock(self.h, sid, float(time), float(yield_time), float(final_time),
+                                        int(max_steps)))
+
+    def deactivate(self, sid):
+        check(self.L.agx_pool_deactivate(self.h, sid))
+
+    def advance(self):
+        n = ctypes.c_int32()
+        check(self.L.agx_pool_advance(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stats(self, sid):
+        st = _lib.StepStats()
+        check(self.L.agx_pool_get_stats(self.h, sid, ctypes.byref(st)))
+        return st
+
+    def time_phases(self, reps=2):
+        ms = np.zeros(_lib.PHASE_COUNT)
+        check(self.L.agx_pool_time_phases(self.h, int(reps), ms.ctypes.data_as(_f64p), _lib.PHASE_COUNT))
+        return dict(zip(_lib.PHASES, ms.tolist()))
+
+    @property
+    def grid(self):
+        return int(self.L.agx_pool_grid(self.h))
+
+
+class MixedScenario:
+    """One mixed-precision scenario (a pool of one) with the Scenario interface."""
+
+    CENTROID_IN = ("stage_c", "xmom_c", "ymom_c", "elev_c", "friction_c")
+
+    def __init__(self, mesh, plain_tables, params):
+        self.mesh = mesh
+        self.N = len(mesh)
+        self.B = int(mesh.boundary_length)
+        self.params = params
+        self.tables = pack_mixed(mesh)
+        self.pool = Pool(self.N, max(self.B, 1), 1)
+        self.sid = self.pool.add(mesh, params, self.tables)
+        self._elev_set = False
+
+    def close(self):
+        self.pool.close()
+
+    def field_len(self, name):
+        return 3 * self.N if (name.endswith("_e") or name.endswith("_v")) else (self.B if name.endswith("_b") else self.N)
+
+    def set(self, name, values):
+        if name in self.CENTROID_IN:
+            self.pool.set_field(self.sid, name, values)
+
+    def get(self, name, out=None):
+        n = self.field_len(name)
+        out = np.empty(n) if out is None else out
+        if name.endswith("_b") or name.endswith("_s") or name == "elev_v":
+            if name == "elev_v":
+                v = self.pool.get_field(self.sid, "elev_e")
+                e = v.reshape(-1, 3)
+                out.reshape(-1, 3)[:] = np.stack([e[:, 1] + e[:, 2] - e[:, 0], e[:, 0] + e[:, 2] - e[:, 1],
+                                                  e[:, 0] + e[:, 1] - e[:, 2]], 1)
+                return out
+            out[:] = 0.0       # not kept by the mixed form
+            return out
+        return self.pool.get_field(self.sid, name, out=out)
+
+    def device_ptr(self, name):
+        raise NotImplementedError("device views are provided for the FP64 scenario")
+
+    def set_boundary(self, kind, values):
+        self.pool.set_boundary(self.sid, kind, values)
+
+    def set_boundary_series(self, rows):
+        self.pool.set_boundary_series(self.sid, rows)
+
+    def add_rate(self, indices, rate, factor=1.0):
+        self.pool.add_rate(self.sid, indices, rate, factor)
+
+    def clear_operators(self):
+        self.pool.clear_operators(self.sid)
+
+    def operator_influx(self, op):
+        return self.pool.operator_influx(self.sid, op)
+
+    def distribute(self, with_protect=True):
+        self.pool.distribute(self.sid)
+
+    def protect(self):
+        self.pool.distribute(self.sid)
+        return 0.0
+
+    def update_boundary(self, t):
+        pass   # boundary values are evaluated inside the flux kernel
+
+    def _no_phase(self, *a):
+        raise NotImplementedError("per-phase calls are provided by the FP64 scenario; the mixed form "
+                                  "runs whole steps (evolve / advance_steps)")
+
+    compute_fluxes = compute_forcing = update_conserved = backup = saxpy = _no_phase
+
+    def set_clock(self, time, yield_time, final_time):
+        self._clock = (time, yield_time, final_time)
+
+    def advance(self, max_steps=0):
+        t, y, f = getattr(self, "_clock", (0.0, 1e300, -1.0))
+        self.pool.set_clock(self.sid, t, y, f, max_steps)
+        self.pool.advance()
+        return self.pool.stats(self.sid)
+
+    def stats(self):
+        return self.pool.stats(self.sid)
+
+    def set_stream(self, ptr):
+        self.pool.set_stream(ptr)
+
+    def time_phases(self, reps=2):
+        return self.pool.time_phases(reps)

@@ -133,3 +133,158 @@ def pack_tables(mesh, tri_full_flag=None, per_side_edges=None, order=None):
                 areas=np.ascontiguousarray(np.asarray(mesh.areas, np.float64)),
                 inv_area=np.ascontiguousarray(inv_area), boundary_slot=np.ascontiguousarray(bslot),
                 vertex_coordinates=np.ascontiguousarray(np.asarray(mesh.vertex_coordinates, np.float64).ravel()))
+
+
+def morton_order(points, bits=16):
+    """Cell order along a Morton (Z-order) curve of the centroids, so that
+    tiles of consecutive cells are compact patches of the mesh."""
+    P = np.asarray(points, np.float64)
+    lo = P.min(axis=0)
+    span = np.maximum(P.max(axis=0) - lo, 1e-300)
+    q = np.clip(((P - lo) / span * ((1 << bits) - 1)).astype(np.uint64), 0, (1 << bits) - 1)
+
+    def spread(v):
+        v = v & np.uint64(0xFFFF)
+        v = (v | (v << np.uint64(8))) & np.uint64(0x00FF00FF)
+        v = (v | (v << np.uint64(4))) & np.uint64(0x0F0F0F0F)
+        v = (v | (v << np.uint64(2))) & np.uint64(0x33333333)
+        v = (v | (v << np.uint64(1))) & np.uint64(0x55555555)
+        return v
+    key = spread(q[:, 0]) | (spread(q[:, 1]) << np.uint64(1))
+    return np.argsort(key, kind="stable")
+
+
+def pack_mixed(mesh, order=None):
+    """FP32 tables of the mixed-precision form, cells in Morton order.
+
+    Returns conn int32 [N,4] (neighbours in the stored order, boundary edges as
+    -(m+1) with the mesh's boundary index m, meta word), geo float32 [N,16]
+    (jump matrix M row-major in g0.xyzw g1.xyzw g2.x, edge vectors in
+    g2.yzw g3.xyz, radius in g3.w), area [N], order [N] (original index of each
+    stored cell) and boundary_cell [B] (stored index).
+
+    The jump matrix maps the differences to the three surrogate neighbours,
+    Dq_j = q_{s_j} - q_k, to the provisional edge jumps; it is the linear
+    gradient of sw_domain_openmp.c:1445-1484 (auxiliary triangle, one boundary
+    or none) or :1684-1696 (two boundaries) evaluated at the edge midpoints.
+    """
+    N = len(mesh)
+    nb = np.asarray(mesh.neighbours, np.int64)
+    ne = np.asarray(mesh.neighbour_edges, np.int64)
+    sn = np.asarray(mesh.surrogate_neighbours, np.int64)
+    nbnd = np.asarray(mesh.number_of_boundaries, np.int64)
+    cells = np.arange(N, dtype=np.int64)
+    expected = np.where(nb >= 0, nb, cells[:, None])
+    if not np.array_equal(expected, sn):
+        raise NotImplementedError("the mixed-precision form needs surrogate neighbours equal to the "
+                                  "flux neighbours (no internal boundary segments)")
+    if order is None:
+        order = morton_order(mesh.centroid_coordinates)
+    order = np.asarray(order, np.int64)
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    C = np.asarray(mesh.centroid_coordinates, np.float64)
+    Em = np.asarray(mesh.edge_midpoint_coordinates, np.float64).reshape(N, 3, 2)
+    V = np.asarray(mesh.vertex_coordinates, np.float64).reshape(N, 3, 2)
+    dxv = Em[:, :, 0] - C[:, 0:1]
+    dyv = Em[:, :, 1] - C[:, 1:2]
+    M = np.zeros((N, 3, 3))
+    x0, y0 = C[sn[:, 0], 0], C[sn[:, 0], 1]
+    x1, y1 = C[sn[:, 1], 0], C[sn[:, 1], 1]
+    x2, y2 = C[sn[:, 2], 0], C[sn[:, 2], 1]
+    dx1, dx2, dy1, dy2 = x1 - x0, x2 - x0, y1 - y0, y2 - y0
+    area2 = dy2 * dx1 - dy1 * dx2
+    typ = nbnd <= 1
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ia2 = np.where(typ, 1.0 / area2, 0.0)
+    cx = np.stack([dy1 - dy2, dy2, -dy1], axis=1) * ia2[:, None]
+    cy = np.stack([dx2 - dx1, -dx2, dx1], axis=1) * ia2[:, None]
+    for i in range(3):
+        M[:, i, :] = cx * dxv[:, i:i + 1] + cy * dyv[:, i:i + 1]
+    M[~typ] = 0.0
+    two = np.nonzero(nbnd == 2)[0]
+    if two.size:
+        s = sn[two]
+        j = np.where(s[:, 0] != two, 0, np.where(s[:, 1] != two, 1, 2))
+        kn = s[np.arange(two.size), j]
+        ddx = C[kn, 0] - C[two, 0]
+        ddy = C[kn, 1] - C[two, 1]
+        dist2 = ddx * ddx + ddy * ddy
+        gdx = ddx / dist2
+        gdy = ddy / dist2
+        for i in range(3):
+            M[two, i, j] = gdx * dxv[two, i] + gdy * dyv[two, i]
+    ev = np.stack([V[:, 2] - V[:, 1], V[:, 0] - V[:, 2], V[:, 1] - V[:, 0]], axis=1)   # [N,3,2]
+    geo = np.zeros((N, 16), np.float32)
+    Mf = M.reshape(N, 9)
+    geo[:, 0:9] = Mf
+    geo[:, 9] = ev[:, 0, 0]
+    geo[:, 10] = ev[:, 0, 1]
+    geo[:, 11] = ev[:, 1, 0]
+    geo[:, 12] = ev[:, 1, 1]
+    geo[:, 13] = ev[:, 2, 0]
+    geo[:, 14] = ev[:, 2, 1]
+    geo[:, 15] = np.asarray(mesh.radii, np.float64)
+    meta = np.zeros(N, np.int64)
+    for i in range(3):
+        meta |= (np.where(nb[:, i] >= 0, ne[:, i], 0) & 3) << (2 * i)
+    meta |= 1 << 8
+    meta |= (nbnd & 3) << 16
+    conn = np.empty((N, 4), np.int64)
+    nbr_new = np.where(nb >= 0, inv[np.where(nb >= 0, nb, 0)], nb)
+    conn[:, :3] = nbr_new
+    conn[:, 3] = meta
+    bcell = inv[np.asarray(mesh.boundary_cells, np.int64)]
+    conn_s = np.ascontiguousarray(conn[order].astype(np.int32))
+    lnk, hoff, hcnt, hcells = tile_halos(conn_s)
+    return dict(conn=conn_s, lnk=lnk, halo_off=hoff, halo_cnt=hcnt, halo_cells=hcells,
+                geo=np.ascontiguousarray(geo[order]),
+                area=np.ascontiguousarray(np.asarray(mesh.areas, np.float64)[order]),
+                order=np.ascontiguousarray(order.astype(np.int32)),
+                boundary_cell=np.ascontiguousarray(bcell.astype(np.int32)))
+
+
+TILE = 256
+HALO_MAX = 256          # halo cells a tile can stage in shared memory
+LNK_INLINE = 1023       # local index meaning "reconstruct this neighbour inline"
+
+
+def tile_halos(conn, tile=TILE, halo_max=HALO_MAX):
+    """Per tile of `tile` consecutive cells: the outside cells whose edges the
+    tile's fluxes need (its halo), and for every cell slot the local index of
+    the neighbour in the tile's staging area (own cells 0..tile-1, halo cells
+    tile..tile+H-1, boundary edges LNK_INLINE, packed 10 bits per slot).
+
+    Returns (lnk int32 [N], halo_off int32 [T], halo_cnt int32 [T],
+    halo_cells int32 [sum H])."""
+    N = conn.shape[0]
+    T = (N + tile - 1) // tile
+    nbr = conn[:, :3].astype(np.int64)
+    cells = np.arange(N, dtype=np.int64)
+    tcell = cells // tile
+    local = np.full((N, 3), LNK_INLINE, np.int64)
+    inside = (nbr >= 0) & (nbr // tile == tcell[:, None])
+    local[inside] = (nbr - (tcell * tile)[:, None])[inside]
+    ext = (nbr >= 0) & ~inside
+    ek, ei = np.nonzero(ext)
+    et = tcell[ek]
+    en = nbr[ek, ei]
+    key = et * (N + 1) + en
+    uk, inv = np.unique(key, return_inverse=True)
+    ut = uk // (N + 1)
+    un = uk % (N + 1)
+    cnt = np.bincount(ut, minlength=T)
+    off = np.zeros(T, np.int64)
+    off[1:] = np.cumsum(cnt)[:-1]
+    pos = np.arange(uk.size) - off[ut]           # position of each halo cell in its tile's list
+    hpos = pos[inv]
+    ok = hpos < halo_max
+    local[ek[ok], ei[ok]] = tile + hpos[ok]
+    lnk = local[:, 0] | (local[:, 1] << 10) | (local[:, 2] << 20)
+    cnt_clamped = np.minimum(cnt, halo_max)
+    # keep only the first halo_max cells of each tile (the rest are reconstructed inline)
+    keep = pos < halo_max
+    hc = un[keep]
+    off2 = np.zeros(T, np.int64)
+    off2[1:] = np.cumsum(cnt_clamped)[:-1]
+    return (lnk.astype(np.int32), off2.astype(np.int32), cnt_clamped.astype(np.int32), hc.astype(np.int32))

@@ -86,3 +86,54 @@ def inflow_bumps(m=1000, L=1.0e4, seed=1234, dry_fraction=0.30, flow_algorithm="
                     "top": Reflective_boundary(d), "bottom": Reflective_boundary(d)})
     d.workload_info = dict(slope=slope, seed=seed, dry_fraction=float(np.mean(slope * cxx + cb > 0.0)))
     return d
+
+
+def batch_sizes(count=256, seed=42, lo=20, hi=400, target=20.0e6, tol=0.05, max_draws=1000):
+    """Mesh sides m_i = round(exp(U(log lo, log hi))), redrawn with the same
+    generator until sum(4 m_i^2) is within tol of target.  Returns (sides, draw)."""
+    rng = np.random.default_rng(seed)
+    for draw in range(max_draws):
+        m = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(int)
+        if abs(4 * np.sum(m * m) - target) <= tol * target:
+            return m, draw
+    raise RuntimeError("no draw within tolerance")
+
+
+def batch_scenario(m, seed, kind, precision="mixed"):
+    """One scenario of the batched workload: rectangular cross m x m over
+    10m x 10m metres, slope + 8 Gaussian bumps, dam break (stage = bed + 1 m
+    for x < L/2) or Dirichlet inflow (stage 1.5 m west), Manning U(0.02, 0.05), DE1."""
+    rng = np.random.default_rng(seed)
+    L = 10.0 * m
+    p, e, b = rectangular_cross(m, m, L, L)
+    d = Domain(p, e, b)
+    d.set_flow_algorithm("DE1")
+    d.set_gpu_options(precision=precision)
+    d.set_store(False)
+    cx = rng.uniform(0, L, 8)
+    cy = rng.uniform(0, L, 8)
+    A = rng.uniform(-2, 2, 8)
+    s = rng.uniform(0.05 * L, 0.2 * L, 8)
+    slope = rng.uniform(0.001, 0.005)
+    zn = -slope * p[:, 0] + _bump_field(p[:, 0], p[:, 1], (cx, cy, A, s))
+    tri = d.mesh.triangles
+    d.set_quantity("elevation", zn[tri].reshape(-1, 3))
+    zc = d.quantities["elevation"].centroid_values
+    xc = d.mesh.centroid_coordinates[:, 0]
+    if kind == "dam":
+        d.set_quantity("stage", zc + np.where(xc < 0.5 * L, 1.0, 0.0), location="centroids")
+        Br = Reflective_boundary(d)
+        d.set_boundary({"left": Br, "right": Br, "top": Br, "bottom": Br})
+    else:
+        d.set_quantity("stage", zc, location="centroids")       # dry; filled from the west
+        d.set_boundary({"left": Dirichlet_boundary([1.5, 0.0, 0.0]), "right": Transmissive_boundary(d),
+                        "top": Reflective_boundary(d), "bottom": Reflective_boundary(d)})
+    d.set_quantity("friction", rng.uniform(0.02, 0.05, len(d)), location="centroids")
+    return d
+
+
+def batch_workload(count=256, seed=42, precision="mixed", target=20.0e6):
+    sides, draw = batch_sizes(count, seed, target=target)
+    doms = [batch_scenario(int(m), seed * 1000 + i, "dam" if i % 2 == 0 else "inflow", precision)
+            for i, m in enumerate(sides)]
+    return doms, dict(sides=sides.tolist(), draw=draw, cells=int(4 * np.sum(sides * sides)))

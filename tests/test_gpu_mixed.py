@@ -1,0 +1,106 @@
+"""Mixed-precision form (FP32 reconstruction and flux, FP64 accumulation,
+FP64 depth and timestep reduction) against the FP64 oracle.
+
+Stated bars: max depth error <= 1 mm against the FP64 oracle over the run;
+water volume of a closed domain conserved to 1e-6 relative; a scenario gives
+bitwise the same result alone and batched with others in one pool.
+"""
+import numpy as np
+import pytest
+
+from anuga_core_gb300 import workloads
+from anuga_core_gb300.mesh import Mesh, rectangular_cross
+from anuga_core_gb300.mixed import Pool
+from helpers import make_domain, make_oracle, random_state
+
+pytestmark = pytest.mark.gpu
+
+DEPTH_TOL = 1.0e-3   # metres
+
+
+def _oracle_for(oracle_mod, d, alg, kinds):
+    Q = d.quantities
+    st = dict(stage=Q["stage"].centroid_values.copy(), xmom=Q["xmomentum"].centroid_values.copy(),
+              ymom=Q["ymomentum"].centroid_values.copy(), elevation=Q["elevation"].centroid_values.copy(),
+              friction=Q["friction"].centroid_values.copy())
+    return make_oracle(oracle_mod, d.mesh, alg, st, kinds), st
+
+
+def test_inflow_bumps_depth_error_within_1mm(oracle_mod):
+    d = workloads.inflow_bumps(m=60, L=600.0, precision="mixed")
+    kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+             "top": ("reflective", None), "bottom": ("reflective", None)}
+    od, _ = _oracle_for(oracle_mod, d, "DE1", kinds)
+    for _ in d.evolve(yieldstep=10.0, finaltime=60.0):
+        pass
+    for _ in od.evolve(yieldstep=10.0, finaltime=60.0):
+        pass
+    z = d.quantities["elevation"].centroid_values
+    h_gpu = np.maximum(d.quantities["stage"].centroid_values - z, 0)
+    h_ref = np.maximum(od.stage_c - od.bed_c, 0)
+    err = np.abs(h_gpu - h_ref).max()
+    assert err <= DEPTH_TOL, err
+    assert abs(d.total_steps - od.total_steps) <= max(2, od.total_steps // 50)
+
+
+def test_dam_break_de0_depth_error_within_1mm(oracle_mod):
+    d = workloads.dam_break(m=40, precision="mixed")
+    kinds = {t: ("reflective", None) for t in ("left", "right", "top", "bottom")}
+    od, _ = _oracle_for(oracle_mod, d, "DE0", kinds)
+    for _ in d.evolve(yieldstep=1.0, finaltime=5.0):
+        pass
+    for _ in od.evolve(yieldstep=1.0, finaltime=5.0):
+        pass
+    z = d.quantities["elevation"].centroid_values
+    err = np.abs(np.maximum(d.quantities["stage"].centroid_values - z, 0) - np.maximum(od.stage_c - od.bed_c, 0)).max()
+    assert err <= DEPTH_TOL, err
+
+
+def test_closed_domain_conserves_volume():
+    d = workloads.dam_break(m=40, flow_algorithm="DE1", precision="mixed")
+    v0 = d.get_water_volume()
+    for _ in d.evolve(yieldstep=2.0, finaltime=10.0):
+        pass
+    v1 = d.get_water_volume()
+    assert abs(v1 - v0) / v0 <= 1e-6, (v0, v1)
+
+
+def test_rain_adds_the_expected_volume():
+    d = workloads.dam_break(m=30, flow_algorithm="DE1", precision="mixed")
+    import anuga_core_gb300 as agx
+    c = d.get_centroid_coordinates()
+    idx = np.nonzero((c[:, 0] > 20) & (c[:, 0] < 60))[0]
+    rate = 0.002
+    agx.Rate_operator(d, rate=rate, indices=idx)
+    v0 = d.get_water_volume()
+    for _ in d.evolve(yieldstep=1.0, finaltime=4.0):
+        pass
+    v1 = d.get_water_volume()
+    expect = rate * 4.0 * d.mesh.areas[idx].sum()
+    assert abs((v1 - v0) - expect) / expect <= 1e-5
+
+
+def _pool_case(seed, m):
+    p, e, b = rectangular_cross(m, m, 10.0 * m, 10.0 * m)
+    mesh = Mesh(p, e, b)
+    st = random_state(mesh, seed)
+    kinds = {"left": ("dirichlet", (float(np.max(st["stage"])) + 0.1, 0.0, 0.0)), "right": ("transmissive", None),
+             "top": ("reflective", None), "bottom": ("reflective", None)}
+    return p, e, b, st, kinds
+
+
+def test_scenario_same_alone_and_batched():
+    cases = [_pool_case(s, m) for s, m in ((1, 12), (2, 30), (3, 7), (4, 21))]
+    alone = []
+    for p, e, b, st, kinds in cases:
+        d = make_domain(p, e, b, "DE1", st, kinds, precision="mixed")
+        d.advance_steps(25)
+        alone.append(d.quantities["stage"].centroid_values.copy())
+    # batched: all four in one pool, advanced by the same graph launches
+    doms = [make_domain(p, e, b, "DE1", st, kinds, precision="mixed") for p, e, b, st, kinds in cases]
+    from anuga_core_gb300.batch import Batch
+    B = Batch(doms)
+    B.advance_steps(25)
+    for i, d in enumerate(doms):
+        got = B.get_centroids(i)["stage_c"]
+        assert np.array_equal(got, alone[i]), i
