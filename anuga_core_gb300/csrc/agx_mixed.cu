@@ -149,31 +149,27 @@ __device__ __forceinline__ float4 protect_prep(const MParams& P, double& w, doub
 }
 
 // ---- reconstruction of one cell's three edges (FP32, relative form) -------
-__device__ __forceinline__ void reconstruct(const PoolDev& d, const MParams& P, int c, const float4* W,
-                                            EdgeState out[3], bool& sdry, float4& rc) {
-  const int4 cn = d.conn[c];
-  const int meta = cn.w;
+// Core of the reconstruction: the cell's own work record rc and those of its
+// three surrogate neighbours r0..r2 (self where a slot is a boundary edge:
+// b0..b2 true).
+__device__ __forceinline__ void reconstruct_core(const PoolDev& d, const MParams& P, int c, int meta,
+                                                 const float4 rc, const float4 r0, const float4 r1,
+                                                 const float4 r2, bool b0, bool b1, bool b2,
+                                                 EdgeState out[3], bool& sdry) {
   const int nb = nb_of(meta);
-  rc = W[c];
-  const int s0 = cn.x >= 0 ? cn.x : c;
-  const int s1 = cn.y >= 0 ? cn.y : c;
-  const int s2 = cn.z >= 0 ? cn.z : c;
-  const float4 r0 = s0 != c ? W[s0] : rc;
-  const float4 r1 = s1 != c ? W[s1] : rc;
-  const float4 r2 = s2 != c ? W[s2] : rc;
   const float hk = rc.x;
-  sdry = ((r0.x < P.hmin) | (s0 == c)) & ((r1.x < P.hmin) | (s1 == c)) & ((r2.x < P.hmin) | (s2 == c));
+  sdry = ((r0.x < P.hmin) | b0) & ((r1.x < P.hmin) | b1) & ((r2.x < P.hmin) | b2);
   float uk = rc.y, vk = rc.z;
   if (sdry) { uk = 0.0f; vk = 0.0f; }
   const float4 a = d.g0[c], b = d.g1[c], e = d.g2[c], f4 = d.g4[c];
   const float M[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, e.x};
   float Dh[3] = {r0.x - hk, r1.x - hk, r2.x - hk};
   float Dw[3] = {f4.x + Dh[0], f4.y + Dh[1], f4.z + Dh[2]};
-  float Du[3] = {s0 != c ? r0.y - uk : 0.0f, s1 != c ? r1.y - uk : 0.0f, s2 != c ? r2.y - uk : 0.0f};
-  float Dv[3] = {s0 != c ? r0.z - vk : 0.0f, s1 != c ? r1.z - vk : 0.0f, s2 != c ? r2.z - vk : 0.0f};
-  if (s0 == c) { Dh[0] = 0.0f; Dw[0] = 0.0f; }
-  if (s1 == c) { Dh[1] = 0.0f; Dw[1] = 0.0f; }
-  if (s2 == c) { Dh[2] = 0.0f; Dw[2] = 0.0f; }
+  float Du[3] = {!b0 ? r0.y - uk : 0.0f, !b1 ? r1.y - uk : 0.0f, !b2 ? r2.y - uk : 0.0f};
+  float Dv[3] = {!b0 ? r0.z - vk : 0.0f, !b1 ? r1.z - vk : 0.0f, !b2 ? r2.z - vk : 0.0f};
+  if (b0) { Dh[0] = 0.0f; Dw[0] = 0.0f; }
+  if (b1) { Dh[1] = 0.0f; Dw[1] = 0.0f; }
+  if (b2) { Dh[2] = 0.0f; Dw[2] = 0.0f; }
   float bw, bu, bv;
   if (nb <= 1) {
     const float hlo = fminf(fminf(r0.x, fminf(r1.x, r2.x)), hk);
@@ -205,6 +201,18 @@ __device__ __forceinline__ void reconstruct(const PoolDev& d, const MParams& P, 
     }
     out[i].dz = Jw[i] - Jh[i];
   }
+}
+
+// Reconstruction of cell c gathering the work records from global memory.
+__device__ __forceinline__ void reconstruct(const PoolDev& d, const MParams& P, int c, const float4* W,
+                                            EdgeState out[3], bool& sdry, float4& rc) {
+  const int4 cn = d.conn[c];
+  rc = W[c];
+  const bool b0 = cn.x < 0, b1 = cn.y < 0, b2 = cn.z < 0;
+  const float4 r0 = b0 ? rc : W[cn.x];
+  const float4 r1 = b1 ? rc : W[cn.y];
+  const float4 r2 = b2 ? rc : W[cn.z];
+  reconstruct_core(d, P, c, cn.w, rc, r0, r1, r2, b0, b1, b2, out, sdry);
 }
 
 __device__ void series_at(const double* rows, int n, double t, double out[3]) {
@@ -291,7 +299,7 @@ __device__ __forceinline__ float4 record_of(const MParams& P, double depth, doub
 // accumulated into the FP64 state with one FP64 add per quantity.
 // Returns 1 if the cell was fixed as negative; depth1 = w - z afterwards.
 __device__ __forceinline__ int update_lean(const MParams& P, double& w, double& uh, double& vh, double z,
-                                           double area, float eta, float4 Ek, double dt, float dt32,
+                                           const double* area, float eta, float4 Ek, double dt, float dt32,
                                            double& added, double& depth1) {
   const double depth = w - z;
   const float h = d2f_bits(depth);
@@ -300,7 +308,7 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& w, double& 
     uh = 0.0;
     vh = 0.0;
     if (negative_bits(depth)) {
-      added = -depth * area;
+      added = -depth * (*area);
       w = z;
     }
   }
@@ -349,8 +357,8 @@ __device__ float block_sum_f(float x, float* sh) {
 // cells (the outside neighbours its edges need) into shared memory; phase 2
 // evaluates the three edge fluxes of every own cell from shared memory and
 // accumulates them.  FUSED2: stage 2 of RK2 (update and combine fused in).
-template <bool FUSED2>
-__global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
+template <bool FUSED2, int MINB>
+__global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
   __shared__ float shf[TILE / 32];
   __shared__ double shd[TILE / 32];
@@ -368,15 +376,24 @@ __global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
     bool sdry = false;
     float4 rk = make_float4(0.f, 0.f, 0.f, 0.f);
     EdgeState own[3];
+    const int2 ht = d.tile_halo[tile];
+    int4 cn = make_int4(-1, -1, -1, 0);
+    int lk = 0;
     if (valid) {
-      reconstruct(d, P, k, W, own, sdry, rk);
+      cn = d.conn[k];
+      lk = d.lnk[k];
+      rk = W[k];
+      const bool b0 = cn.x < 0, b1 = cn.y < 0, b2 = cn.z < 0;
+      const float4 r0 = b0 ? rk : W[cn.x];
+      const float4 r1 = b1 ? rk : W[cn.y];
+      const float4 r2 = b2 ? rk : W[cn.z];
+      reconstruct_core(d, P, k, cn.w, rk, r0, r1, r2, b0, b1, b2, own, sdry);
     } else {
 #pragma unroll
       for (int i = 0; i < 3; i++) own[i] = EdgeState{0.f, 0.f, 0.f, 0.f};
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) es[threadIdx.x * 3 + i] = own[i];
-    const int2 ht = d.tile_halo[tile];
     for (int h = threadIdx.x; h < ht.y; h += TILE) {
       EdgeState hs[3];
       bool sd;
@@ -388,9 +405,15 @@ __global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
     __syncthreads();
     float ew = 0.f, ex = 0.f, ey = 0.f, smax = 0.f, bfl = 0.f;
     float4 g3 = make_float4(0.f, 0.f, 0.f, 0.f), g4 = g3;
+    // the FP64 state of the fused update is loaded before the flux loop
+    double sw = 0.0, suh = 0.0, svh = 0.0, zk = 0.0;
+    if (FUSED2 && valid) {
+      sw = d.wB[k];
+      suh = d.uhB[k];
+      svh = d.vhB[k];
+      zk = d.z[k];
+    }
     if (valid) {
-      const int4 cn = d.conn[k];
-      const int lk = d.lnk[k];
       const float4 g2 = d.g2[k];
       g3 = d.g3[k];
       g4 = d.g4[k];
@@ -499,16 +522,19 @@ __global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
       }
       const float bm = block_min_f(dtk, shf);
       const float bs = block_sum_f(bfl, shf);
-      if (threadIdx.x == 0) d.tile_red1[tile] = make_float2(bm, bs);
+      if (threadIdx.x == 0) {      // fire-and-forget reductions (no return value)
+        if (bm < 3.0e38f) atomicMax(&S->clock.dt_key, ~(unsigned long long)__double_as_longlong((double)bm));
+        if (bs != 0.0f) atomicAdd(&S->clock.bfs_acc, (double)bs);
+      }
     } else {
       int neg = 0;
       double added = 0.0;
       if (valid) {
         const double dt = S->clock.timestep;
-        double w = d.wB[k], uh = d.uhB[k], vh = d.vhB[k];
-        const double z = d.z[k];
+        double w = sw, uh = suh, vh = svh;
+        const double z = zk;
         double depth1;
-        neg = update_lean(P, w, uh, vh, z, d.area[k], d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f), dt,
+        neg = update_lean(P, w, uh, vh, z, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f), dt,
                           (float)dt, added, depth1);
         w = 0.5 * w + 0.5 * d.wA[k];
         uh = 0.5 * uh + 0.5 * d.uhA[k];
@@ -523,7 +549,7 @@ __global__ void __launch_bounds__(TILE, 3) k_pool_flux(PoolDev d) {
       const double ma = anym ? block_sum_d(added, shd) : 0.0;
       const int nneg = __syncthreads_count(neg);
       if (threadIdx.x == 0) {
-        d.tile_red2[tile] = bs;
+        if (bs != 0.0f) atomicAdd(&S->clock.bfs[1], (double)bs);
         if (ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
         if (nneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)nneg);
       }
@@ -552,7 +578,7 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
       double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
       const double z = d.z[k];
       double depth1;
-      neg = update_lean(P, w, uh, vh, z, d.area[k], d.eta[k], d.E[k], dt, (float)dt, added, depth1);
+      neg = update_lean(P, w, uh, vh, z, d.area + k, d.eta[k], d.E[k], dt, (float)dt, added, depth1);
       const float4 r = record_of(P, depth1, uh, vh);
       if (euler) {
         d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh;
@@ -651,31 +677,14 @@ __global__ void k_pool_edges(PoolDev d, int sid, double* we, double* he, double*
   }
 }
 
-// update_timestep per scenario: one block reduces the scenario's tile
-// partials (minimum radius/speed as an FP64 key, boundary flux) and applies
-// the CFL/clamp logic.
+// update_timestep per scenario (one thread each).
 __global__ void k_pool_timestep(PoolDev d, int nscn) {
-  __shared__ float shf[TILE / 32];
-  __shared__ double shd[TILE / 32];
-  const int s = blockIdx.x;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nscn) return;
   PoolScn* S = d.scn + s;
   if (!S->alive || !S->active) return;
-  float m = 3.0e38f;
-  double b = 0.0;
-  for (int t = S->tile0 + threadIdx.x; t < S->tile0 + S->ntile; t += blockDim.x) {
-    const float2 r = d.tile_red1[t];
-    m = fminf(m, r.x);
-    b += (double)r.y;
-  }
-  m = block_min_f(m, shf);
-  b = block_sum_d(b, shd);
-  if (threadIdx.x == 0) {
-    S->clock.dt_key = m < 3.0e38f ? ~(unsigned long long)__double_as_longlong((double)m) : 0ull;
-    S->clock.bfs_acc = b;
-    S->clock.bfs[0] = b;
-    timestep_logic(&S->clock);
-  }
+  S->clock.bfs[0] = S->clock.bfs_acc;
+  timestep_logic(&S->clock);
 }
 
 __global__ void k_pool_reset(PoolDev d, int nscn) {
@@ -684,6 +693,7 @@ __global__ void k_pool_reset(PoolDev d, int nscn) {
   PoolScn* S = d.scn + s;
   S->clock.dt_key = 0ull;
   S->clock.bfs_acc = 0.0;
+  S->clock.bfs[1] = 0.0;
 }
 
 struct PoolOp {
@@ -718,40 +728,19 @@ __global__ void k_pool_rate(PoolDev d, PoolOp op, int slot) {
   if (slot < MAX_OPS) atomicAdd(&S->clock.op_influx[slot], infl);
 }
 
-// Per-scenario clocks, one block each: stage-2 boundary flux reduction and
-// the end-of-step bookkeeping.  The last block to finish (ticket) sets the
-// graph's while condition when any scenario is still running.
+// Per-scenario clocks (one thread each, one block); sets the graph's while
+// condition when any scenario is still running.
 __global__ void k_pool_clock(PoolDev d, int nscn, cudaGraphConditionalHandle handle, int set_cond) {
-  __shared__ double shd[TILE / 32];
-  const int s = blockIdx.x;
-  PoolScn* S = d.scn + s;
-  const bool act = S->alive && S->active;
   int running = 0;
-  if (act) {
-    double b = 0.0;
-    if (S->P.rk2)
-      for (int t = S->tile0 + threadIdx.x; t < S->tile0 + S->ntile; t += blockDim.x) b += (double)d.tile_red2[t];
-    b = block_sum_d(b, shd);
-    if (threadIdx.x == 0) {
-      S->clock.bfs[1] = b;
-      const int reason = clock_logic(&S->clock);
-      if (reason) S->active = 0;
-      else running = 1;
-    }
+  for (int s = threadIdx.x; s < nscn; s += blockDim.x) {
+    PoolScn* S = d.scn + s;
+    if (!S->alive || !S->active) continue;
+    const int reason = clock_logic(&S->clock);
+    if (reason) S->active = 0;
+    else running = 1;
   }
-  if (threadIdx.x == 0) {
-    if (running) atomicAdd(&d.ctl[0], 1u);
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&d.ctl[1], 1u);
-    if (ticket == (unsigned int)nscn - 1u) {
-      __threadfence();
-      const unsigned int any = atomicAdd(&d.ctl[0], 0u);
-      d.ctl[0] = 0u;
-      d.ctl[1] = 0u;
-      __threadfence();
-      if (set_cond) cudaGraphSetConditional(handle, any ? 1u : 0u);
-    }
-  }
+  const int any = __syncthreads_or(running);
+  if (threadIdx.x == 0 && set_cond) cudaGraphSetConditional(handle, any ? 1u : 0u);
 }
 
 __global__ void k_gather(double* dst, const double* src, const int* order, int n) {
@@ -792,6 +781,7 @@ struct ScnHost {
   double* series = nullptr;
   std::vector<PoolOp> ops;
   bool work_dirty = true;
+  bool running = false;          // serving: still has steps to take towards its final time
 };
 
 struct Pool {
@@ -813,6 +803,11 @@ struct Pool {
   cudaGraphExec_t exec = nullptr;
   bool graph_valid = false;
   int grid = 0;
+  int grid_v[2] = {0, 0};        // persistent grid per flux variant
+  int variant = 0;               // flux kernel variant: 0 = 80 registers (3 blocks/SM), 1 = 64 registers
+  int grid_mode = 0;             // 0 = persistent grid, 1 = one block per tile
+  void* snap = nullptr;          // snapshot of the dynamic state (autotuning, checkpoints)
+  size_t snap_bytes = 0;
   int kernels_per_iter = 0;
   int mode_rk2_any = 1;
 };
@@ -935,10 +930,12 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   const int S = p->cap_scn;
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
-  k_pool_flux<false><<<G, TILE, 0, st>>>(d);
+  const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
+  if (p->variant == 0) k_pool_flux<false, 3><<<Gf, TILE, 0, st>>>(d);
+  else k_pool_flux<false, 4><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
-  k_pool_timestep<<<S, TILE, 0, st>>>(d, S);
+  k_pool_timestep<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   phase_mark(st, PH_SMALL);
   // RK2 scenarios: update1 into B + flux2 fused; Euler scenarios only update.
@@ -947,7 +944,8 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   k_pool_update<<<std::max(d.ntiles, 1), TILE, 0, st>>>(d, 0);
   count_launch();
   phase_mark(st, PH_UPDATE);
-  k_pool_flux<true><<<G, TILE, 0, st>>>(d);
+  if (p->variant == 0) k_pool_flux<true, 3><<<Gf, TILE, 0, st>>>(d);
+  else k_pool_flux<true, 4><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
   for (size_t s = 0; s < p->scn.size(); s++) {
@@ -960,7 +958,7 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
       phase_mark(st, PH_RATE);
     }
   }
-  k_pool_clock<<<S, TILE, 0, st>>>(d, S, (cudaGraphConditionalHandle)h, set_cond ? 1 : 0);
+  k_pool_clock<<<1, 1024, 0, st>>>(d, S, (cudaGraphConditionalHandle)h, set_cond ? 1 : 0);
   count_launch();
   phase_mark(st, PH_SMALL);
   return cudaGetLastError();
@@ -1034,10 +1032,13 @@ agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
   PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, p->stream));
   agx_status st = push_scn(p);
   if (st) return st;
-  int sms = 0, per = 0;
+  int sms = 0, per = 0, per4 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false, 3>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pool_flux<false, 4>, TILE, 0);
   p->grid = std::max(1, sms * std::max(per, 1));
+  p->grid_v[0] = p->grid;
+  p->grid_v[1] = std::max(1, sms * std::max(per4, 1));
   *out = p;
   return AGX_OK;
 }
@@ -1068,6 +1069,7 @@ agx_status agx_pool_destroy(agx_pool p) {
     for (auto& op : s.ops) if (op.idx) cudaFree((void*)op.idx);
   }
   if (p->arena) cudaFree(p->arena);
+  if (p->snap) cudaFree(p->snap);
   if (p->scn_host) cudaFreeHost(p->scn_host);
   if (p->own_stream) cudaStreamDestroy(p->own_stream);
   delete p;
@@ -1460,6 +1462,7 @@ agx_status agx_pool_set_clock(agx_pool p, int32_t sid, double time, double yield
   c.recorded_min = p->scn[sid].prm.evolve_max_timestep;
   c.recorded_max = p->scn[sid].prm.evolve_min_timestep;
   p->scn_host[sid].active = 1;
+  p->scn[sid].running = true;
   return push_scn(p);
 }
 
@@ -1576,6 +1579,140 @@ agx_status agx_pool_time_phases(agx_pool p, int32_t reps, double* ms, int32_t n_
 }
 
 int32_t agx_pool_grid(agx_pool p) { return p ? p->grid : 0; }
+
+// Continuous batching: give every running scenario up to max_steps more
+// steps (stopping early at its final or yield time) and launch the device
+// loop without waiting.  agx_pool_wait completes the call.
+agx_status agx_pool_launch_chunk(agx_pool p, int64_t max_steps) {
+  if (!p || max_steps <= 0) return pfail(AGX_E_INVALID, "bad arguments");
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn[s].alive && p->scn[s].running) { agx_status st = ensure_work(p, s); if (st) return st; }
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  int nact = 0;
+  for (int s = 0; s < p->cap_scn; s++) {
+    PoolScn& S = p->scn_host[s];
+    if (!p->scn[s].alive || !p->scn[s].running) continue;
+    S.clock.steps_call = 0;
+    S.clock.steps_target = max_steps;
+    S.clock.reason = 0;
+    S.active = 1;
+    nact++;
+  }
+  if ((st = push_scn(p))) return st;
+  if (nact == 0) return AGX_OK;
+  if (!p->graph_valid && (st = pool_build_graph(p)) != AGX_OK) return st;
+  PCK(cudaGraphLaunch(p->exec, p->stream));
+  return AGX_OK;
+}
+
+// Wait for the launched chunk; scenarios that reached their final time (or
+// failed) stop running.  Returns how many are still running.
+agx_status agx_pool_wait(agx_pool p, int32_t* n_running) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  long long iters = 0;
+  int run = 0;
+  for (int s = 0; s < p->cap_scn; s++) {
+    if (!p->scn[s].alive) continue;
+    const Clock& c = p->scn_host[s].clock;
+    iters = std::max(iters, c.steps_call);
+    if (p->scn[s].running && (c.reason == AGX_STOP_FINAL || c.reason == AGX_STOP_ERROR || c.error))
+      p->scn[s].running = false;
+    if (p->scn[s].running) run++;
+  }
+  count_launch(iters * p->kernels_per_iter);
+  if (n_running) *n_running = run;
+  return AGX_OK;
+}
+
+// Statistics of n scenarios with one device read.  running[i] is 1 while the
+// scenario still has steps to take.
+agx_status agx_pool_stats_all(agx_pool p, int32_t n, const int32_t* sids, agx_step_stats* out, int32_t* running) {
+  if (!p || n < 0 || (n && (!sids || !out))) return pfail(AGX_E_INVALID, "bad arguments");
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  for (int i = 0; i < n; i++) {
+    const int s = sids[i];
+    if (s < 0 || s >= p->cap_scn || !p->scn[s].alive) return pfail(AGX_E_INVALID, "bad scenario %d", s);
+    fill_stats_p(&p->scn_host[s].clock, out + i);
+    if (running) running[i] = p->scn[s].running ? 1 : 0;
+  }
+  return AGX_OK;
+}
+
+// Free capacity: cells (tile granular), boundary slots, halo slots, scenario slots.
+agx_status agx_pool_capacity(agx_pool p, int64_t* free_cells, int64_t* free_boundary, int64_t* free_halo,
+                             int32_t* free_scenarios) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  int64_t fc = 0, run = 0, fb = 0, rb = 0, fh = 0, rh = 0;
+  for (int t = 0; t < p->cap_tiles; t++) { run = p->tile_scn[t] < 0 ? run + 1 : 0; fc = std::max(fc, run); }
+  for (int b = 0; b < p->cap_bnd; b++) { rb = p->bnd_owner[b] < 0 ? rb + 1 : 0; fb = std::max(fb, rb); }
+  for (int h = 0; h < p->cap_halo; h++) { rh = p->halo_owner[h] < 0 ? rh + 1 : 0; fh = std::max(fh, rh); }
+  int fs = 0;
+  for (int s = 0; s < p->cap_scn; s++) fs += p->scn[s].alive ? 0 : 1;
+  if (free_cells) *free_cells = fc * TILE;
+  if (free_boundary) *free_boundary = fb;
+  if (free_halo) *free_halo = fh;
+  if (free_scenarios) *free_scenarios = fs;
+  return AGX_OK;
+}
+
+// Kernel variant of the fused flux kernels (0: 80 registers, 3 blocks/SM;
+// 1: 64 registers, 4 blocks/SM) and grid mode (0: persistent, 1: one block
+// per tile).  Chosen by the autotuner.
+agx_status agx_pool_set_variant(agx_pool p, int32_t variant, int32_t grid_mode) {
+  if (!p || variant < 0 || variant > 1 || grid_mode < 0 || grid_mode > 1) return pfail(AGX_E_INVALID, "bad variant");
+  if (p->variant != variant || p->grid_mode != grid_mode) p->graph_valid = false;
+  p->variant = variant;
+  p->grid_mode = grid_mode;
+  return AGX_OK;
+}
+
+// Snapshot / restore of every scenario's dynamic state and clock (device to
+// device copies into a buffer allocated on the first snapshot).
+static agx_status ensure_work(Pool* p, int sid);
+static size_t snap_layout(Pool* p, char* base, bool save) {
+  const size_t C = p->cap_cells;
+  struct Part { void* a; size_t n; } parts[] = {
+      {p->d.wA, C * 8}, {p->d.uhA, C * 8}, {p->d.vhA, C * 8}, {p->d.wB, C * 8}, {p->d.uhB, C * 8},
+      {p->d.vhB, C * 8}, {p->d.W0, C * 16}, {p->d.W1, C * 16}, {p->d.E, C * 16}, {p->d.maxs, C * 4},
+      {p->d.scn, sizeof(PoolScn) * p->cap_scn}};
+  size_t off = 0;
+  for (auto& q : parts) {
+    if (base) {
+      if (save) cudaMemcpyAsync(base + off, q.a, q.n, cudaMemcpyDeviceToDevice, p->stream);
+      else cudaMemcpyAsync(q.a, base + off, q.n, cudaMemcpyDeviceToDevice, p->stream);
+    }
+    off += al(q.n);
+  }
+  return off;
+}
+
+agx_status agx_pool_snapshot(agx_pool p) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  // pending work records belong to the state being saved
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
+  const size_t need = snap_layout(p, nullptr, true);
+  if (!p->snap) {
+    PCK(cudaMalloc(&p->snap, need));
+    p->snap_bytes = need;
+  }
+  snap_layout(p, (char*)p->snap, true);
+  PCK(cudaGetLastError());
+  return psync(p);
+}
+
+agx_status agx_pool_restore(agx_pool p) {
+  if (!p || !p->snap) return pfail(AGX_E_STATE, "no snapshot to restore");
+  snap_layout(p, (char*)p->snap, false);
+  PCK(cudaGetLastError());
+  agx_status st = psync(p);
+  if (st) return st;
+  return pull_scn(p);
+}
 
 int32_t agx_pool_last_error(char* buf, int32_t n) {
   if (buf && n > 0) {

@@ -53,6 +53,14 @@ def lib():
             "agx_pool_operator_influx": ([H, ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
             "agx_pool_time_phases": ([H, ctypes.c_int32, _f64p, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_grid": ([H], ctypes.c_int32),
+            "agx_pool_set_variant": ([H, ctypes.c_int32, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_snapshot": ([H], ctypes.c_int32),
+            "agx_pool_launch_chunk": ([H, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_wait": ([H, P(ctypes.c_int32)], ctypes.c_int32),
+            "agx_pool_stats_all": ([H, ctypes.c_int32, _i32p, P(_lib.StepStats), _i32p], ctypes.c_int32),
+            "agx_pool_capacity": ([H, P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int32)],
+                                  ctypes.c_int32),
+            "agx_pool_restore": ([H], ctypes.c_int32),
             "agx_pool_last_error": ([ctypes.c_char_p, ctypes.c_int32], ctypes.c_int32),
         }
         for name, (args, res) in sig.items():
@@ -193,6 +201,41 @@ class Pool:
     @property
     def grid(self):
         return int(self.L.agx_pool_grid(self.h))
+
+    def set_variant(self, variant, grid_mode):
+        check(self.L.agx_pool_set_variant(self.h, int(variant), int(grid_mode)))
+        self.variant = (int(variant), int(grid_mode))
+
+    def snapshot(self):
+        check(self.L.agx_pool_snapshot(self.h))
+
+    def restore(self):
+        check(self.L.agx_pool_restore(self.h))
+
+    def scenarios(self):
+        return sorted(self._keep)
+
+    def launch_chunk(self, max_steps):
+        check(self.L.agx_pool_launch_chunk(self.h, int(max_steps)))
+
+    def wait(self):
+        n = ctypes.c_int32()
+        check(self.L.agx_pool_wait(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stats_all(self, sids):
+        n = len(sids)
+        arr = (_lib.StepStats * max(n, 1))()
+        ids = np.ascontiguousarray(sids, np.int32)
+        run = np.zeros(max(n, 1), np.int32)
+        check(self.L.agx_pool_stats_all(self.h, n, ids.ctypes.data_as(_i32p), arr, run.ctypes.data_as(_i32p)))
+        return [arr[i] for i in range(n)], run[:n].astype(bool)
+
+    def capacity(self):
+        fc, fb, fh = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        fs = ctypes.c_int32()
+        check(self.L.agx_pool_capacity(self.h, ctypes.byref(fc), ctypes.byref(fb), ctypes.byref(fh), ctypes.byref(fs)))
+        return dict(cells=fc.value, boundary=fb.value, halo=fh.value, scenarios=fs.value)
 
 
 class MixedScenario:

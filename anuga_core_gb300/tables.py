@@ -179,7 +179,7 @@ def pack_mixed(mesh, order=None):
         raise NotImplementedError("the mixed-precision form needs surrogate neighbours equal to the "
                                   "flux neighbours (no internal boundary segments)")
     if order is None:
-        order = morton_order(mesh.centroid_coordinates)
+        order, _name, _costs = best_order(mesh)
     order = np.asarray(order, np.int64)
     inv = np.empty(N, np.int64)
     inv[order] = np.arange(N)
@@ -288,3 +288,51 @@ def tile_halos(conn, tile=TILE, halo_max=HALO_MAX):
     off2 = np.zeros(T, np.int64)
     off2[1:] = np.cumsum(cnt_clamped)[:-1]
     return (lnk.astype(np.int32), off2.astype(np.int32), cnt_clamped.astype(np.int32), hc.astype(np.int32))
+
+
+def hilbert_order(points, bits=16):
+    """Cell order along a Hilbert curve of the centroids (better locality
+    than Morton: consecutive cells are always adjacent patches)."""
+    P = np.asarray(points, np.float64)
+    lo = P.min(axis=0)
+    span = np.maximum(P.max(axis=0) - lo, 1e-300)
+    n = 1 << bits
+    x = np.clip(((P[:, 0] - lo[0]) / span[0] * (n - 1)).astype(np.int64), 0, n - 1)
+    y = np.clip(((P[:, 1] - lo[1]) / span[1] * (n - 1)).astype(np.int64), 0, n - 1)
+    d = np.zeros(len(P), np.int64)
+    s = n // 2
+    while s > 0:
+        rx = (x & s) > 0
+        ry = (y & s) > 0
+        d += s * s * ((3 * rx) ^ ry)
+        # rotate the quadrant
+        flip = ~ry
+        swap_x = np.where(flip & rx, s - 1 - x, x)
+        swap_y = np.where(flip & rx, s - 1 - y, y)
+        x = np.where(flip, swap_y, swap_x)
+        y = np.where(flip, swap_x, swap_y)
+        s //= 2
+    return np.argsort(d, kind="stable")
+
+
+def halo_cost(mesh, order, tile=TILE):
+    """Fraction of extra reconstructions (halo cells per own cell) of an order."""
+    N = len(mesh)
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    nb = np.asarray(mesh.neighbours, np.int64)[order]
+    conn = np.where(nb >= 0, inv[np.where(nb >= 0, nb, 0)], -1)
+    k = np.arange(N)[:, None]
+    ext = (conn >= 0) & (conn // tile != k // tile)
+    pairs = np.unique((k // tile * (N + 1) + conn)[ext])
+    return pairs.size / max(N, 1)
+
+
+def best_order(mesh, tile=TILE):
+    """The cheaper of the Morton and Hilbert orders by halo cost (the
+    reordering choice of the autotuner); returns (order, name, costs)."""
+    C = mesh.centroid_coordinates
+    cands = {"hilbert": hilbert_order(C), "morton": morton_order(C)}
+    costs = {k: halo_cost(mesh, v, tile) for k, v in cands.items()}
+    name = min(costs, key=costs.get)
+    return cands[name], name, costs

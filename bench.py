@@ -196,6 +196,11 @@ def main():
     stream = torch.cuda.Stream()          # a real stream: the legacy default one has handle 0
     torch.cuda.set_stream(stream)
     scn.set_stream(stream.cuda_stream)
+    tune = None
+    if args.precision == "mixed":
+        from anuga_core_gb300.autotune import tune_pool
+        res, best = tune_pool(scn.pool, steps=5, reps=2)
+        tune = {"chosen": best, "s_per_step": res}
     d.advance_steps(args.warmup)
     launches0 = _lib.kernel_launches()
 
@@ -266,7 +271,7 @@ def main():
             "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2, %s" %
                        (args.m, args.m, N, args.precision), "cells": N, "precision": args.precision,
                        "l2": "inputs larger than L2 (state %.0f MB)" % (scn_bytes(d) / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single", "autotune": tune},
             "roofline": {"bound": "hbm", "achieved": achieved_step, "peak": hbm, "unit": "GB/s",
                          "frac": achieved_step / hbm, "peak_kind": peak_kind,
                          "traffic": None, "kernel": "whole step (%s dominant: %.1f%% of step time)" %
@@ -299,6 +304,8 @@ def run_batch(args, torch, rank, world, local, dist):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     B.set_stream(stream.cuda_stream)
+    from anuga_core_gb300.autotune import tune_pool
+    res, best = tune_pool(B.pool, steps=3, reps=2)
     B.advance_steps(args.warmup)
     launches0 = _lib.kernel_launches()
     sampler = ClockSampler(local)
@@ -322,7 +329,8 @@ def run_batch(args, torch, rank, world, local, dist):
             "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
             "config": {"workload": "batch of %d rectangular-cross scenarios, sides log-uniform [20,400], %d triangles, "
                        "DE1 mixed, one pool" % (len(doms), N), "cells": N, "scenarios": len(doms),
-                       "setup_s": setup_s, "draw": info["draw"], "l2": "inputs larger than L2"},
+                       "setup_s": setup_s, "draw": info["draw"], "l2": "inputs larger than L2",
+                       "autotune": {"chosen": best, "s_per_step": res}},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                          "peak_kind": peak_kind, "traffic": None, "phase_ms": phases},
             "gpu_launches": int(launches), "clocks": clocks}

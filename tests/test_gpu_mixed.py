@@ -104,3 +104,29 @@ def test_scenario_same_alone_and_batched():
     for i, d in enumerate(doms):
         got = B.get_centroids(i)["stage_c"]
         assert np.array_equal(got, alone[i]), i
+
+
+def test_snapshot_restore_and_autotune_leave_state_unchanged():
+    p, e, b, st, kinds = _pool_case(9, 24)
+    d1 = make_domain(p, e, b, "DE1", st, kinds, precision="mixed")
+    d1.advance_steps(10)
+    ref = d1.quantities["stage"].centroid_values.copy()
+    d2 = make_domain(p, e, b, "DE1", st, kinds, precision="mixed")
+    d2._ensure_device()
+    from anuga_core_gb300.autotune import tune_pool, VARIANTS
+    pool = d2._scn.pool
+    res, best = tune_pool(pool, steps=3, reps=1)
+    assert set(res) == {"r80-persistent", "r80-per-tile", "r64-persistent", "r64-per-tile"}
+    d2.advance_steps(10)
+    got = d2.quantities["stage"].centroid_values
+    assert np.array_equal(got, ref)
+    # every kernel variant computes the same result
+    outs = []
+    for v in VARIANTS:
+        d3 = make_domain(p, e, b, "DE1", st, kinds, precision="mixed")
+        d3._ensure_device()
+        d3._scn.pool.set_variant(*v)
+        d3.advance_steps(10)
+        outs.append(d3.quantities["stage"].centroid_values.copy())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])

@@ -52,3 +52,42 @@ def test_low_froude_forces_per_side_evaluation():
     T = pack_tables(mesh, per_side_edges=np.ones((len(mesh), 3), bool))
     assert np.all(T["edge_opp"] == -1)
     assert T["edge_slot"].size == 3 * len(mesh)
+
+
+@pytest.mark.parametrize("mesh", [Mesh(*rectangular_cross(60, 50, 60.0, 50.0)), _delaunay(3000, 4)],
+                         ids=["rect", "delaunay"])
+def test_mixed_tables_and_tile_halos(mesh):
+    from anuga_core_gb300.tables import pack_mixed, TILE, LNK_INLINE
+    T = pack_mixed(mesh)
+    N = len(mesh)
+    order = T["order"]
+    assert np.array_equal(np.sort(order), np.arange(N))
+    conn = T["conn"]
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    # neighbours are the mesh's, renumbered
+    nb = mesh.neighbours[order]
+    assert np.array_equal(conn[:, :3][nb >= 0], inv[nb[nb >= 0]])
+    lnk, off, cnt, hc = T["lnk"], T["halo_off"], T["halo_cnt"], T["halo_cells"]
+    for k in range(0, N, 7):
+        t = k // TILE
+        for i in range(3):
+            li = (int(lnk[k]) >> (10 * i)) & 1023
+            n = conn[k, i]
+            if n < 0:
+                assert li == LNK_INLINE
+            elif li < TILE:
+                assert n == t * TILE + li
+            elif li != LNK_INLINE:
+                assert hc[off[t] + li - TILE] == n
+    # the jump matrix reproduces a linear field exactly at the edge midpoints
+    C = mesh.centroid_coordinates[order]
+    E = mesh.edge_midpoint_coordinates.reshape(-1, 3, 2)[order]
+    f = lambda x, y: 0.3 * x - 0.7 * y
+    M = T["geo"][:, :9].astype(np.float64).reshape(-1, 3, 3)
+    s = np.where(conn[:, :3] >= 0, conn[:, :3], np.arange(N)[:, None])
+    D = f(C[s, 0], C[s, 1]) - f(C[:, 0], C[:, 1])[:, None]
+    J = np.einsum("kij,kj->ki", M, D)
+    exact = f(E[:, :, 0], E[:, :, 1]) - f(C[:, 0], C[:, 1])[:, None]
+    typical = mesh.number_of_boundaries[order] == 0
+    assert np.allclose(J[typical], exact[typical], atol=1e-4 * (1 + np.abs(exact[typical]).max()))
