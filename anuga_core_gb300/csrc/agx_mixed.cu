@@ -22,6 +22,7 @@
 // formed in FP64 and rounded once; fluxes and reconstruction are FP32.
 #include "agx_internal.cuh"
 #include "de_mixed.cuh"
+#include "../../include/agx_pool.h"
 #include <algorithm>
 #include <cstdarg>
 #include <cstring>
@@ -870,7 +871,6 @@ static size_t pool_layout(Pool* p, char* base) {
 using namespace agx;
 
 struct agx_pool_s : public agx::Pool {};
-typedef agx_pool_s* agx_pool;
 
 static agx_status psync(Pool* p) {
   PCK(cudaStreamSynchronize(p->stream));

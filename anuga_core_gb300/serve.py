@@ -56,30 +56,31 @@ def _size_ladder(lo=1.0e4, hi=2.0e6, steps=12):
 
 def delaunay_mesh(n_cells, seed, spacing=10.0):
     """Delaunay triangulation of a jittered lattice in a square (about
-    n_cells triangles); boundary edges on the west side are tagged 'inflow',
-    the others 'wall'."""
+    n_cells triangles).  Interior points move by up to 0.3 spacing; points on
+    the square's sides stay on the lattice, so no triangle degenerates along
+    the boundary.  Boundary edges on the west side are tagged 'inflow', the
+    others 'wall'."""
     from scipy.spatial import Delaunay
     rng = np.random.default_rng(seed)
     npts = max(int(n_cells // 2), 16)
-    side = int(np.ceil(np.sqrt(npts)))
-    L = side * spacing
+    side = max(int(np.ceil(np.sqrt(npts))), 3)
+    L = (side - 1) * spacing
     gx, gy = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
     pts = np.stack([gx.ravel(), gy.ravel()], 1).astype(float) * spacing
-    pts += rng.uniform(-0.3, 0.3, pts.shape) * spacing
-    pts = np.clip(pts, 0.0, L - spacing)
+    interior = (gx.ravel() > 0) & (gx.ravel() < side - 1) & (gy.ravel() > 0) & (gy.ravel() < side - 1)
+    pts[interior] += rng.uniform(-0.3, 0.3, (int(interior.sum()), 2)) * spacing
     tri = Delaunay(pts).simplices.astype(np.int64)
     a = pts[tri]
     cr = (a[:, 1, 0] - a[:, 0, 0]) * (a[:, 2, 1] - a[:, 0, 1]) - (a[:, 1, 1] - a[:, 0, 1]) * (a[:, 2, 0] - a[:, 0, 0])
-    keep = np.abs(cr) > 1e-9 * spacing * spacing
+    keep = np.abs(cr) > 1e-6 * spacing * spacing
     tri = tri[keep]
     cr = cr[keep]
     tri[cr < 0] = tri[cr < 0][:, [0, 2, 1]]
     M0 = Mesh(pts, tri)
-    xmin = pts[:, 0].min()
     bnd = {}
     E = M0.edge_midpoint_coordinates.reshape(-1, 3, 2)
     for (v, e) in M0.boundary:
-        bnd[(v, e)] = "inflow" if E[v, e, 0] < xmin + 0.02 * L else "wall"
+        bnd[(v, e)] = "inflow" if E[v, e, 0] < 0.01 * L else "wall"
     return Mesh(pts, tri, bnd)
 
 
@@ -231,6 +232,7 @@ class FloodServer:
                 self.pool.get_field(sid, "stage_c")       # the result read (D2H) is part of the latency
             t_done = time.perf_counter() - t0
             if st.reason == _lib.STOP_ERROR:
+                self.pool.stats(sid)                      # raises with the device's error
                 raise _lib.AgxError(-5, "scenario %d failed on the device" % req.rid)
             self.results.append(Result(req.rid, n, int(st.total_steps), req.arrival, t_adm, t_done, stage))
             self.cell_steps += n * int(st.total_steps)
@@ -238,7 +240,9 @@ class FloodServer:
 
     def run(self, requests, realtime=True, max_wall=None):
         """Serve the requests; returns a summary dict (p50/p99 latency,
-        aggregate cell-steps/s)."""
+        aggregate cell-steps/s).  realtime=True admits a request once its
+        arrival time has passed on the wall clock; realtime=False replays the
+        stream as fast as possible, every request counting as arrived."""
         pending = sorted(requests, key=lambda r: r.arrival)
         futures = {}
         t0 = time.perf_counter()
@@ -256,7 +260,9 @@ class FloodServer:
                 i_next += 1
             for rid in sorted(futures, key=lambda k: futures[k][0].arrival):
                 r, f = futures[rid]
-                if f.done() and r.arrival <= clock:
+                # replay mode (realtime=False) takes requests strictly in arrival
+                # order, so admission does not depend on host thread timing
+                if (f.done() or not realtime) and r.arrival <= clock:
                     waiting.append(f.result())
                     del futures[rid]
             waiting.sort(key=lambda p: p[0].arrival)

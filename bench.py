@@ -9,6 +9,11 @@ the 129 MB L2, so no explicit flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+By default the plain FP64 path and then the mixed-precision path run on the
+same workload; the line's value, roofline and e2e are the mixed path's, and
+`plain_fp64` holds the plain path's figures (`mixed_over_plain` = ratio).
+`--workload batch` and `--workload serve` run the batched and serving forms.
+
 `--impl reference` times the CPU oracle (the restated reference algorithm,
 OpenMP over all host cores) on a bounded sample of the same workload.
 """
@@ -102,9 +107,7 @@ def build_workload(m, precision):
     return d
 
 
-def cpu_baseline(m, steps, threads):
-    """Oracle (restated reference, OpenMP) on the same workload: `steps` DE1
-    steps of the full mesh after one warm-up step."""
+def _oracle_domain(m, threads):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from anuga_core_gb300 import workloads
@@ -120,41 +123,51 @@ def cpu_baseline(m, steps, threads):
     kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
              "top": ("reflective", None), "bottom": ("reflective", None)}
     od.set_boundaries([(d.mesh.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in d.mesh.tag_boundary_cells])
-    gen = od.evolve(yieldstep=1e9, finaltime=None, max_steps=steps + 1)
+    gen = od.evolve(yieldstep=1e9, finaltime=None, max_steps=10**9)
     next(gen)                      # initial distribute
     od.relative_yieldtime = 1e300
     od.relative_finaltime = None
     od.rk2_step(1e300, None)       # warm-up step
+    return od, len(d.mesh)
+
+
+def _oracle_steps(od, steps):
     t0 = time.perf_counter()
     for _ in range(steps):
         od.rk2_step(1e300, None)
         od.relative_time += od.timestep
-    el = time.perf_counter() - t0
-    N = len(d.mesh)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(m, steps, threads):
+    """Oracle (restated reference, OpenMP) on the same workload: `steps` DE1
+    steps of the full mesh after one warm-up step."""
+    od, N = _oracle_domain(m, threads)
+    el = _oracle_steps(od, steps)
     return {"value": N * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d DE1 steps of the %d-triangle inflow_bumps mesh (%.1f s)" % (steps, N, el)}
 
 
 def run_reference(args):
+    """The oracle port (the reference's CPU algorithm, OpenMP on every host
+    core); one bench step = one DE1 step of the full mesh."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    per_step = []
-    base = None
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(args.m, args.cpu_steps, threads)
-        if i >= args.warmup:
-            per_step.append(r["value"])
-        base = r
-    v = float(np.median(per_step)) if per_step else base["value"]
+    od, N = _oracle_domain(args.m, threads)
+    _oracle_steps(od, args.warmup)
+    el = _oracle_steps(od, args.steps)
+    v = N * args.steps / el
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (4 * args.m * args.m) / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2" %
-                       (args.m, args.m, 4 * args.m * args.m), "l2": "inputs larger than L2"},
-            "cpu_baseline": dict(base, value=v),
+                       (args.m, args.m, N), "cells": N, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d DE1 steps of the full %d-triangle mesh after %d warm-up steps (%.1f s)"
+                             % (args.steps, N, args.warmup, el)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -166,10 +179,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--m", type=int, default=1000, help="mesh side (4*m*m triangles)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--cpu-steps", type=int, default=3, dest="cpu_steps")
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"],
+                    help="both: plain FP64 then mixed on the same workload; the line's value is mixed")
+    ap.add_argument("--cpu-steps", type=int, default=60, dest="cpu_steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="inflow_bumps", choices=["inflow_bumps", "batch"],
+    ap.add_argument("--requests", type=int, default=64, help="serve workload: number of requests")
+    ap.add_argument("--workload", default="inflow_bumps", choices=["inflow_bumps", "batch", "serve"],
                     help="inflow_bumps: one 4M-triangle mesh; batch: 256 scenarios (~20M triangles) in one pool")
     ap.add_argument("--batch-count", type=int, default=256, dest="batch_count")
     args = ap.parse_args()
@@ -189,20 +204,9 @@ def main():
     from anuga_core_gb300 import _lib
     if args.workload == "batch":
         return run_batch(args, torch, rank, world, local, dist)
-    d = build_workload(args.m, args.precision)
-    N = len(d)
-    d.distribute_to_vertices_and_edges()
-    scn = d._scn
-    stream = torch.cuda.Stream()          # a real stream: the legacy default one has handle 0
-    torch.cuda.set_stream(stream)
-    scn.set_stream(stream.cuda_stream)
-    tune = None
-    if args.precision == "mixed":
-        from anuga_core_gb300.autotune import tune_pool
-        res, best = tune_pool(scn.pool, steps=5, reps=2)
-        tune = {"chosen": best, "s_per_step": res}
-    d.advance_steps(args.warmup)
-    launches0 = _lib.kernel_launches()
+    if args.workload == "serve":
+        return run_serve(args, torch)
+    precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
 
     def barrier():
         if dist is not None:
@@ -211,14 +215,79 @@ def main():
 
     sampler = ClockSampler(local)
     sampler.start()
+    res = {}
+    for prec in precisions:
+        res[prec] = measure_single(args, prec, torch, world, barrier, dist)
+    clocks = sampler.stop()
+    if rank == 0:
+        head = res[precisions[-1]]
+        N = head["cells"]
+        cpu = None
+        if not args.no_cpu and world == 1:
+            cpu = cpu_baseline(args.m, args.cpu_steps, os.cpu_count() or 1)
+        line = {
+            "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head["precision"] == "fp64" else "f32 flux / f64 accumulate",
+            "data": "synthetic",
+            "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2" %
+                       (args.m, args.m, N), "cells": N, "precision": head["precision"],
+                       "l2": "inputs larger than L2 (state %.0f MB)" % (head["state_bytes"] / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single", "autotune": head["autotune"]},
+            "roofline": head["roofline"],
+            "step_roofline": head["step_roofline"],
+            "e2e": head["e2e"],
+            "gpu_launches": int(sum(r["launches"] for r in res.values())),
+            "clocks": clocks,
+        }
+        if "fp64" in res and head["precision"] != "fp64":
+            pf = res["fp64"]
+            line["plain_fp64"] = {k: pf[k] for k in ("value", "ms_per_step", "roofline", "step_roofline", "e2e")}
+            line["mixed_over_plain"] = head["value"] / pf["value"]
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# Compulsory bytes per cell and step of the dominant kernel category, for
+# the per-kernel roofline (the arrays each kernel must read or write once).
+# mixed "flux": stage-1 flux (static 96 + lnk 4 + record 16 read, E 20
+# written) + stage-2 flux (168 read, 40 written).  mixed "update": 60 read,
+# 40 written.  fp64 "extrap", per RK2 stage: conn and surr (32), extrapolation
+# geometry (11 x 8), centroid w, h, u, v (32) read; edge w, h, uh, vh, z
+# (5 x 3 x 8) written.
+KERNEL_BYTES_PER_CELL = {"mixed": {"flux": 136.0 + 208.0, "update": 100.0},
+                         "fp64": {"extrap": 2 * 272.0}}
+
+
+def measure_single(args, precision, torch, world, barrier, dist):
+    """Device-resident throughput, per-kernel roofline and the end-to-end
+    figure (host buffers through the C ABI) of one precision form."""
+    from anuga_core_gb300 import _lib
+    d = build_workload(args.m, precision)
+    N = len(d)
+    d.distribute_to_vertices_and_edges()
+    scn = d._scn
+    stream = torch.cuda.Stream()          # a real stream: the legacy default one has handle 0
+    torch.cuda.set_stream(stream)
+    scn.set_stream(stream.cuda_stream)
+    tune = None
+    if precision == "mixed":
+        from anuga_core_gb300.autotune import tune_pool
+        res, best = tune_pool(scn.pool, steps=5, reps=2)
+        tune = {"chosen": best, "s_per_step": res}
+    d.advance_steps(args.warmup)
+    launches0 = _lib.kernel_launches()
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    st = d.advance_steps(args.steps)
+    d.advance_steps(args.steps)
     e1.record(stream)
     barrier()
-    clocks = sampler.stop()
     ms = e0.elapsed_time(e1)
     launches = _lib.kernel_launches() - launches0
     if dist is not None:
@@ -228,13 +297,30 @@ def main():
     ms_per_step = ms / args.steps
     value = world * N * args.steps / (ms / 1e3)
 
-    # per-kernel event timing (direct launches) for the roofline
+    # per-kernel CUDA-event timing (direct launches on the same stream)
     phases = scn.time_phases(reps=3)
     step_ms = sum(phases.values())
-    dominant = max(phases, key=phases.get)
     hbm, peak_kind = _peaks()
-    alg_bytes_step = ALG_BYTES_PER_CELL_STEP[args.precision] * N
-    achieved_step = alg_bytes_step / (ms_per_step / 1e3) / 1e9
+    kb = KERNEL_BYTES_PER_CELL[precision]
+    dominant = max(phases, key=phases.get)
+    dom_bytes = kb.get(dominant)
+    ach_k = dom_bytes * N / (phases[dominant] / 1e3) / 1e9 if dom_bytes else None
+    roof = {"bound": "hbm", "achieved": ach_k, "peak": hbm, "unit": "GB/s",
+            "frac": ach_k / hbm if ach_k else None, "peak_kind": peak_kind,
+            "traffic": TRAFFIC_PER_STEP.get((precision, dominant), {}).get("bytes_per_cell", None),
+            "kernel": "%s (%.1f%% of step time)" % (dominant, 100.0 * phases[dominant] / max(step_ms, 1e-9)),
+            "kernel_ms_per_step": phases[dominant], "alg_bytes_per_cell": dom_bytes,
+            "phase_ms": phases}
+    if roof["traffic"] is not None:
+        roof["traffic"] = roof["traffic"] * N
+        roof["traffic_note"] = TRAFFIC_PER_STEP[(precision, dominant)]["note"]
+    if precision == "fp64":
+        roof["note"] = "FP64-pipe bound (DFMA ~0.5 T/s on GB300); HBM fraction reported for reference"
+    alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
+    ach_s = alg_step / (ms_per_step / 1e3) / 1e9
+    step_roof = {"achieved": ach_s, "peak": hbm, "unit": "GB/s", "frac": ach_s / hbm,
+                 "note": "%d algorithmic B/cell-step of the ideal fused step x cells / step time" %
+                 ALG_BYTES_PER_CELL_STEP[precision]}
 
     # e2e: through the C ABI with host buffers, copies inside the timed region
     pin = {f: torch.empty(N, dtype=torch.float64, pin_memory=True).numpy() for f in ("stage_c", "xmom_c", "ymom_c")}
@@ -256,38 +342,18 @@ def main():
     barrier()
     e2e_ms = e2.elapsed_time(e3)
     e2e_value = world * N * args.steps / (e2e_ms / 1e3)
+    out = {"precision": precision, "cells": N, "value": value, "ms_per_step": ms_per_step, "roofline": roof,
+           "step_roofline": step_roof, "launches": launches, "autotune": tune, "state_bytes": scn_bytes(d),
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N}}
+    del d, scn
+    torch.cuda.synchronize()
+    return out
 
-    if rank == 0:
-        cpu = None
-        if not args.no_cpu and world == 1:
-            cpu = cpu_baseline(args.m, args.cpu_steps, os.cpu_count() or 1)
-        dom_ms = phases[dominant]
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32 flux / f64 accumulate",
-            "data": "synthetic",
-            "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2, %s" %
-                       (args.m, args.m, N, args.precision), "cells": N, "precision": args.precision,
-                       "l2": "inputs larger than L2 (state %.0f MB)" % (scn_bytes(d) / 1e6),
-                       "parallelism": "replicas" if world > 1 else "single", "autotune": tune},
-            "roofline": {"bound": "hbm", "achieved": achieved_step, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved_step / hbm, "peak_kind": peak_kind,
-                         "traffic": None, "kernel": "whole step (%s dominant: %.1f%% of step time)" %
-                         (dominant, 100.0 * dom_ms / max(step_ms, 1e-9)),
-                         "phase_ms": phases,
-                         "note": "achieved = %d algorithmic B/cell-step x cells / step time" %
-                         ALG_BYTES_PER_CELL_STEP[args.precision]},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N},
-            "gpu_launches": int(launches),
-            "clocks": clocks,
-        }
-        if cpu is not None:
-            line["cpu_baseline"] = cpu
-        print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+
+# DRAM traffic per cell-step of the dominant kernel category, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum summed over that
+# category's launches of one step, divided by the cells of the captured mesh).
+TRAFFIC_PER_STEP = {}
 
 
 def run_batch(args, torch, rank, world, local, dist):
@@ -334,6 +400,35 @@ def run_batch(args, torch, rank, world, local, dist):
             "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                          "peak_kind": peak_kind, "traffic": None, "phase_ms": phases},
             "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line))
+
+
+def run_serve(args, torch):
+    """Poisson stream (20 req/s, seed 99) of flood scenarios: rectangular cross
+    or Delaunay meshes with 10k-2M triangles (log-uniform), final times
+    U(60, 3600) s, mixed precision, continuous batching in one pool.  The
+    first `--requests` requests of the stream are served in real time."""
+    from anuga_core_gb300.serve import FloodServer, MeshCache, poisson_requests
+    reqs = poisson_requests(n=args.requests)
+    cache = MeshCache()
+    t0 = time.time()
+    for r in reqs:                 # build the meshes of the stream up front (mesh cache warm)
+        cache.get(r.kind, r.cells)
+    setup_s = time.time() - t0
+    srv = FloodServer(max_scenarios=256, chunk_steps=64, mesh_cache=cache)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    summ = srv.run(reqs, realtime=True)
+    clocks = sampler.stop()
+    srv.close()
+    line = {"metric": METRIC, "value": summ["cell_steps_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": summ["requests"], "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
+            "config": {"workload": "serving: %d Poisson requests (20/s), 10k-2M triangles, final time 60-3600 s, "
+                       "DE1 mixed, continuous batching" % len(reqs), "mesh_setup_s": setup_s},
+            "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
+                        "cell_steps": summ["cell_steps"]},
+            "clocks": clocks}
     print(json.dumps(line))
 
 

@@ -9,7 +9,7 @@
  * Every routine states the reference function it follows (paths relative to
  * the anuga_core project).  Arithmetic is written in the same operation order
  * as the reference so that, compiled with -ffp-contract=off, results are
- * bit-identical to the reference built the same way (see oracle/test_ref.py).
+ * bit-identical to the reference built the same way (tests/test_oracle_ref.py checks this).
  *
  * Serial semantics: the reference's OpenMP extrapolation loop lets a cell
  * zero the centroid velocity of a "surrounded by dry cells" triangle that

@@ -56,6 +56,29 @@ def test_dam_break_de0_depth_error_within_1mm(oracle_mod):
     assert err <= DEPTH_TOL, err
 
 
+def test_delaunay_dry_start_inflow_depth_error_within_1mm(oracle_mod):
+    """Unstructured mesh (jittered-lattice Delaunay), dry start, Dirichlet
+    inflow on the west side and Manning friction: the serving workload's
+    scenario form."""
+    from anuga_core_gb300.serve import Request, delaunay_mesh, scenario_state
+    mesh = delaunay_mesh(8000, seed=3)
+    req = Request(rid=0, arrival=0.0, kind="delaunay", cells=8000, seed=41, finaltime=20.0, inflow_stage=2.0)
+    z, stage, eta = scenario_state(mesh, req)
+    st = dict(elevation=z, stage=stage, xmom=0 * z, ymom=0 * z, friction=eta)
+    kinds = {"inflow": ("dirichlet", (2.0, 0.0, 0.0)), "wall": ("reflective", None)}
+    d = make_domain(mesh.nodes, mesh.triangles, mesh.boundary, "DE1", st, kinds, precision="mixed")
+    od = make_oracle(oracle_mod, mesh, "DE1", st, kinds)
+    for _ in d.evolve(yieldstep=5.0, finaltime=20.0):
+        pass
+    for _ in od.evolve(yieldstep=5.0, finaltime=20.0):
+        pass
+    h_gpu = np.maximum(d.quantities["stage"].centroid_values - z, 0)
+    h_ref = np.maximum(od.stage_c - od.bed_c, 0)
+    assert h_ref.max() > 0.1                       # the inflow has entered
+    err = np.abs(h_gpu - h_ref).max()
+    assert err <= DEPTH_TOL, err
+
+
 def test_closed_domain_conserves_volume():
     d = workloads.dam_break(m=40, flow_algorithm="DE1", precision="mixed")
     v0 = d.get_water_volume()
