@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import concurrent.futures
 import dataclasses
+import threading
 import time
 
 import numpy as np
@@ -85,11 +86,17 @@ def delaunay_mesh(n_cells, seed, spacing=10.0):
 
 
 class MeshCache:
-    """Meshes and their device tables, one per (kind, size on a log ladder)."""
+    """Meshes and their device tables, one per (kind, size on a log ladder).
+
+    Safe to share between the server's preparation threads: each entry is
+    built once, under a lock of its own, and a Delaunay mesh's seed follows
+    from its size, so the same key always gives the same mesh."""
 
     def __init__(self, ladder=None):
         self.ladder = _size_ladder() if ladder is None else np.asarray(ladder)
         self.cache = {}
+        self._lock = threading.Lock()
+        self._key_locks = {}
 
     def snap(self, cells):
         return int(self.ladder[np.argmin(np.abs(np.log(self.ladder) - np.log(cells)))])
@@ -97,15 +104,26 @@ class MeshCache:
     def get(self, kind, cells):
         n = self.snap(cells)
         key = (kind, n)
-        if key not in self.cache:
+        with self._lock:
+            hit = self.cache.get(key)
+            if hit is not None:
+                return hit
+            lock = self._key_locks.setdefault(key, threading.Lock())
+        with lock:
+            with self._lock:
+                hit = self.cache.get(key)
+            if hit is not None:
+                return hit
             if kind == "rect":
                 m = max(int(round(np.sqrt(n / 4.0))), 2)
                 p, e, b = rectangular_cross(m, m, 10.0 * m, 10.0 * m)
                 mesh = Mesh(p, e, b)
             else:
-                mesh = delaunay_mesh(n, seed=len(self.cache) + 7)
-            self.cache[key] = (mesh, pack_mixed(mesh))
-        return self.cache[key]
+                mesh = delaunay_mesh(n, seed=7 + n)
+            entry = (mesh, pack_mixed(mesh))
+            with self._lock:
+                self.cache[key] = entry
+            return entry
 
 
 def scenario_state(mesh, req):

@@ -29,3 +29,26 @@ def test_delaunay_mesh_and_state():
     assert eta.min() >= 0.02 and eta.max() <= 0.05
     c = MeshCache(ladder=[5000.0, 20000.0])
     assert c.snap(6000) == 5000 and c.snap(15000) == 20000
+
+
+def test_delaunay_mesh_is_well_shaped():
+    """No slivers: the smallest inscribed radius stays a fair fraction of the
+    lattice spacing (10 m), so the CFL timestep cannot collapse."""
+    m = delaunay_mesh(20000, seed=5)
+    assert m.radii.min() > 0.5
+    assert m.areas.min() > 5.0
+
+
+def test_mesh_cache_is_shared_safely_between_threads():
+    import threading
+    c = MeshCache(ladder=[5000.0])
+    got = []
+    threads = [threading.Thread(target=lambda: got.append(c.get("delaunay", 5000)[0])) for _ in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert len(got) == 4 and all(g is got[0] for g in got)
+    # the same key gives the same mesh in a fresh cache
+    again = MeshCache(ladder=[5000.0]).get("delaunay", 5000)[0]
+    assert np.array_equal(again.nodes, got[0].nodes)
