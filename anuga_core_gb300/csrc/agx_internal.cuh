@@ -82,16 +82,19 @@ __host__ __device__ inline int clock_logic(Clock* c) {
       !(c->time >= c->yield_time))
     c->error |= ERR_NAN;
   if (c->steps_call >= MAX_STEPS_PER_CALL) c->error |= ERR_STEPCAP;
+  // A step that reaches the final or the yield time reports that even when it
+  // is also the last step of the target count, so the next call does not
+  // take a zero-length step.
   if (c->error) {
     reason = AGX_STOP_ERROR;
-  } else if (c->steps_target > 0 && c->steps_call >= c->steps_target) {
-    reason = AGX_STOP_MAXSTEPS;
   } else if (c->final_time >= 0.0 && c->time >= c->final_time - 1.0e-12) {
     if (c->time > c->final_time) c->error |= ERR_OVERSHOOT;
     c->time = c->final_time;
     reason = AGX_STOP_FINAL;
   } else if (c->time >= c->yield_time) {
     reason = AGX_STOP_YIELD;
+  } else if (c->steps_target > 0 && c->steps_call >= c->steps_target) {
+    reason = AGX_STOP_MAXSTEPS;
   }
   c->reason = reason;
   return reason;

@@ -353,7 +353,13 @@ def measure_single(args, precision, torch, world, barrier, dist):
 # DRAM traffic per cell-step of the dominant kernel category, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum summed over that
 # category's launches of one step, divided by the cells of the captured mesh).
-TRAFFIC_PER_STEP = {}
+TRAFFIC_PER_STEP = {
+    ("mixed", "flux"): {
+        "bytes_per_cell": (117.2096e6 + 10.04544e6 + 177.274112e6 + 24.079616e6) / 1.0e6,
+        "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
+                "(m=500, MINB=3 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
+                "scaled by cells; profiles/k_pool_flux_inflow_bumps_1M_mixed.md"},
+}
 
 
 def run_batch(args, torch, rank, world, local, dist):
