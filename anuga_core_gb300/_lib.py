@@ -111,6 +111,7 @@ def load(path=None):
         "agx_last_error": ([ctypes.c_char_p, ctypes.c_int32], ctypes.c_int32),
         "agx_version": ([], ctypes.c_int32),
         "agx_kernel_launches": ([], ctypes.c_int64),
+        "agx_fp64_throughput": ([_f64p, _f64p, _f64p], ctypes.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -299,6 +300,13 @@ class Scenario:
 
 def kernel_launches():
     return int(load().agx_kernel_launches())
+
+
+def fp64_throughput():
+    """Measured FP64 DFMA / DDIV / DSQRT rates of the current device, G ops/s."""
+    v = [np.zeros(1) for _ in range(3)]
+    check(load().agx_fp64_throughput(*[ptr_f64(a) for a in v]))
+    return {"dfma_gops": float(v[0][0]), "ddiv_gops": float(v[1][0]), "dsqrt_gops": float(v[2][0])}
 
 
 def footprint(n_cells, n_boundary, n_edges, precision=AGX_PREC_FP64):

@@ -29,6 +29,7 @@ UNITS = [
     ("agx_mixed.cu", ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]),
     ("agx_batch.cu", []),
     ("agx_noalloc.cu", ["--fmad=false"]),
+    ("agx_probe.cu", []),
 ]
 
 

@@ -704,11 +704,9 @@ struct PoolOp {
   double rate, factor;
 };
 
-__global__ void k_pool_rate(PoolDev d, PoolOp op, int slot) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  PoolScn* S = d.scn + op.sid;
-  if (!S->active || j >= op.n) return;
-  const int k = op.idx[j];
+// Rate_operator change of one cell of op's index set; returns the influx.
+__device__ __forceinline__ double rate_cell(const PoolDev& d, const PoolOp& op, PoolScn* S) {
+  const int k = op.idx[threadIdx.x + blockIdx.x * blockDim.x];
   const double dt = S->clock.timestep;
   double infl;
   if (op.rate >= 0.0) {
@@ -726,7 +724,26 @@ __global__ void k_pool_rate(PoolDev d, PoolOp op, int slot) {
   }
   double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
   d.W0[k] = protect_prep(S->P, w, uh, vh, d.z[k], d.area[k], added);
-  if (slot < MAX_OPS) atomicAdd(&S->clock.op_influx[slot], infl);
+  return infl;
+}
+
+__global__ void __launch_bounds__(256) k_pool_rate(PoolDev d, PoolOp op, int slot) {
+  __shared__ double part[256 / 32];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  PoolScn* S = d.scn + op.sid;
+  if (!S->active) return;
+  double infl = 0.0;
+  if (j < op.n) infl = rate_cell(d, op, S);
+  // influx: one atomic per block (a single address receives every block's sum)
+  infl = warp_sum_d(infl);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = infl;
+  __syncthreads();
+  if (wid == 0) {
+    double r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    r = warp_sum_d(r);
+    if (lane == 0 && slot < MAX_OPS && r != 0.0) atomicAdd(&S->clock.op_influx[slot], r);
+  }
 }
 
 // Per-scenario clocks (one thread each, one block); sets the graph's while

@@ -10,6 +10,13 @@
                        stage 2 m west, transmissive east, reflective north and
                        south, Manning U(0.02,0.06) per cell, DE1 (4.0M
                        triangles at m=1000).
+* ``rain_polygon``   : unstructured mesh of a seeded 20-vertex random polygon
+                       (Delaunay of a jittered lattice: triangles of at most
+                       50 m^2, at most 12.5 m^2 inside a seeded refined
+                       region), bed = 6-octave value noise in [-10, 30] m,
+                       stage 0, rain 50 mm/h over a 1 km^2 square, Dirichlet
+                       stage 3 m on a 500 m inflow segment, reflective walls,
+                       DE1 (about 1.2M triangles at the default size).
 Each builder returns a configured Domain (store disabled).
 """
 from __future__ import annotations
@@ -17,7 +24,9 @@ from __future__ import annotations
 import numpy as np
 
 from .domain import Domain
-from .mesh import rectangular_cross
+from .geometry import inside_polygon
+from .mesh import Mesh, rectangular_cross
+from .operators import Rate_operator
 from .boundaries import Reflective_boundary, Transmissive_boundary, Dirichlet_boundary
 
 
@@ -137,3 +146,161 @@ def batch_workload(count=256, seed=42, precision="mixed", target=20.0e6):
     doms = [batch_scenario(int(m), seed * 1000 + i, "dam" if i % 2 == 0 else "inflow", precision)
             for i, m in enumerate(sides)]
     return doms, dict(sides=sides.tolist(), draw=draw, cells=int(4 * np.sum(sides * sides)))
+
+
+# ---------------------------------------------------------------------------
+# Unstructured workload: rain and inflow on a random polygon
+
+
+def random_polygon(n_vertices, rng, r_lo=0.55, r_hi=1.0):
+    """Star-shaped (hence simple) polygon: angle-sorted random directions with
+    random radii, counter-clockwise, around the origin."""
+    ang = np.sort(rng.uniform(0.0, 2.0 * np.pi, n_vertices))
+    r = rng.uniform(r_lo, r_hi, n_vertices)
+    return np.stack([r * np.cos(ang), r * np.sin(ang)], 1)
+
+
+def polygon_area(poly):
+    x, y = poly[:, 0], poly[:, 1]
+    return 0.5 * float(np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y))
+
+
+def value_noise(x, y, octaves=6, seed=7, base=4, lo=-10.0, hi=30.0):
+    """Sum of `octaves` octaves of value noise (random values on a 2^k lattice
+    over the points' bounding box, smoothstep-interpolated, amplitude halved
+    per octave), rescaled to [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    u = (x - x.min()) / max(x.max() - x.min(), 1e-12)
+    v = (y - y.min()) / max(y.max() - y.min(), 1e-12)
+    total = np.zeros_like(u)
+    amp = 1.0
+    for o in range(octaves):
+        n = base << o
+        G = rng.uniform(-1.0, 1.0, (n + 1, n + 1))
+        fx, fy = u * n, v * n
+        ix = np.minimum(fx.astype(np.int64), n - 1)
+        iy = np.minimum(fy.astype(np.int64), n - 1)
+        tx, ty = fx - ix, fy - iy
+        sx, sy = tx * tx * (3 - 2 * tx), ty * ty * (3 - 2 * ty)
+        a = G[ix, iy] * (1 - sx) + G[ix + 1, iy] * sx
+        b = G[ix, iy + 1] * (1 - sx) + G[ix + 1, iy + 1] * sx
+        total += amp * (a * (1 - sy) + b * sy)
+        amp *= 0.5
+    t = (total - total.min()) / max(total.max() - total.min(), 1e-12)
+    return lo + (hi - lo) * t
+
+
+def _lattice(x0, x1, y0, y1, h, rng, jitter):
+    nx = int(np.floor((x1 - x0) / h)) + 1
+    ny = int(np.floor((y1 - y0) / h)) + 1
+    gx, gy = np.meshgrid(x0 + h * np.arange(nx), y0 + h * np.arange(ny), indexing="ij")
+    pts = np.stack([gx.ravel(), gy.ravel()], 1)
+    return pts + rng.uniform(-jitter, jitter, pts.shape) * h
+
+
+def polygon_mesh(target_cells=1.2e6, seed=7, max_area=50.0, refine=4.0, n_vertices=20, jitter=0.1,
+                 inflow_length=500.0):
+    """Unstructured triangle mesh of a seeded random polygon with a refined
+    interior region.
+
+    Jittered square lattices (spacing sqrt(2 max_area) / 1.12, so that the
+    jittered halves of a lattice square stay below max_area, and sqrt(refine)
+    times finer inside the refined polygon) are triangulated by Delaunay; triangles
+    whose centroid lies in the outer polygon are kept and oriented
+    counter-clockwise.  Triangles above their area limit get their centroid
+    inserted as a new point and the set is triangulated again (conforming by
+    construction).  The polygon is scaled so that the mesh has about
+    `target_cells` triangles.  Boundary edges within inflow_length / 2 of the
+    polygon's first vertex are tagged 'inflow', the others 'wall'.
+    Returns (mesh, info)."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    outer = random_polygon(n_vertices, rng)
+    c_in = outer.mean(0) * 0.0 + rng.uniform(-0.2, 0.2, 2)
+    inner = random_polygon(8, rng, 0.6, 1.0) * 0.22 + c_in
+    h = np.sqrt(2.0 * max_area) / 1.12
+    hf = h / np.sqrt(refine)
+    a_out, a_in = polygon_area(outer), polygon_area(inner)
+    # cells ~ 2 (A_out - A_in) / h^2 + 2 A_in / hf^2
+    scale = np.sqrt(target_cells * h * h / (2.0 * (a_out + (refine - 1.0) * a_in)))
+    outer *= scale
+    inner *= scale
+    x0, y0 = outer.min(0) - 2 * h
+    x1, y1 = outer.max(0) + 2 * h
+    coarse = _lattice(x0, x1, y0, y1, h, rng, jitter)
+    coarse = np.delete(coarse, inside_polygon(coarse, inner), axis=0)
+    ix0, iy0 = inner.min(0)
+    ix1, iy1 = inner.max(0)
+    fine = _lattice(ix0, ix1, iy0, iy1, hf, rng, jitter)
+    fine = fine[inside_polygon(fine, inner)]
+    pts = np.concatenate([coarse, fine])
+    limit_fine = max_area / refine
+    for _ in range(6):
+        tri = Delaunay(pts).simplices.astype(np.int64)
+        a = pts[tri]
+        cr = (a[:, 1, 0] - a[:, 0, 0]) * (a[:, 2, 1] - a[:, 0, 1]) - (a[:, 1, 1] - a[:, 0, 1]) * (a[:, 2, 0] - a[:, 0, 0])
+        cen = a.mean(1)
+        keep = np.zeros(len(tri), bool)
+        keep[inside_polygon(cen, outer)] = True
+        keep &= np.abs(cr) > 1e-9 * h * h
+        tri, cr, cen = tri[keep], cr[keep], cen[keep]
+        area = 0.5 * np.abs(cr)
+        lim = np.full(len(tri), max_area)
+        lim[inside_polygon(cen, inner)] = limit_fine
+        big = area > lim
+        if not big.any():
+            break
+        pts = np.concatenate([pts, cen[big]])
+    tri[cr < 0] = tri[cr < 0][:, [0, 2, 1]]
+    used = np.unique(tri)
+    remap = -np.ones(len(pts), np.int64)
+    remap[used] = np.arange(len(used))
+    pts = pts[used]
+    tri = remap[tri]
+    M0 = Mesh(pts, tri)
+    E = M0.edge_midpoint_coordinates.reshape(-1, 3, 2)
+    v0 = outer[0]
+    bnd = {}
+    for (vol, e) in M0.boundary:
+        q = E[vol, e]
+        bnd[(vol, e)] = "inflow" if np.hypot(q[0] - v0[0], q[1] - v0[1]) <= 0.5 * inflow_length else "wall"
+    mesh = Mesh(pts, tri, bnd)
+    info = dict(seed=seed, cells=len(mesh), polygon=outer.tolist(), refined=inner.tolist(),
+                area_km2=float(np.sum(mesh.areas)) / 1e6, max_area=float(mesh.areas.max()))
+    return mesh, info
+
+
+_POLYGON_MESHES = {}
+
+
+def rain_polygon(target_cells=1.2e6, seed=7, precision="mixed", flow_algorithm="DE1", rain_mm_per_hour=50.0,
+                 inflow_stage=3.0, patch_km2=1.0):
+    """The unstructured rain-and-inflow scenario (see the module docstring).
+    The mesh of a (target_cells, seed) pair is built once per process."""
+    from .boundaries import Dirichlet_boundary as _D, Reflective_boundary as _R
+    key = (float(target_cells), int(seed))
+    if key not in _POLYGON_MESHES:
+        _POLYGON_MESHES[key] = polygon_mesh(target_cells, seed)
+    mesh, info = _POLYGON_MESHES[key]
+    info = dict(info)
+    d = Domain(mesh.nodes, mesh.triangles, mesh.boundary)
+    d.set_flow_algorithm(flow_algorithm)
+    d.set_gpu_options(precision=precision)
+    d.set_store(False)
+    zn = value_noise(mesh.nodes[:, 0], mesh.nodes[:, 1], seed=seed)
+    d.set_quantity("elevation", zn[mesh.triangles].reshape(-1, 3))
+    d.set_quantity("stage", 0.0)
+    d.set_quantity("friction", 0.03)
+    d.set_boundary({"inflow": _D([inflow_stage, 0.0, 0.0]), "wall": _R(d)})
+    # rain over a 1 km^2 square centred on the cell nearest the polygon's centroid
+    C = mesh.centroid_coordinates
+    c = C[np.argmin(np.hypot(C[:, 0] - C[:, 0].mean(), C[:, 1] - C[:, 1].mean()))]
+    half = 500.0 * np.sqrt(patch_km2)
+    square = [[c[0] - half, c[1] - half], [c[0] + half, c[1] - half], [c[0] + half, c[1] + half],
+              [c[0] - half, c[1] + half]]
+    rate = rain_mm_per_hour / 1000.0 / 3600.0
+    op = Rate_operator(d, rate=rate, polygon=square)
+    info.update(rain_cells=int(op.indices.size), rain_rate=rate, inflow_edges=len(mesh.tag_boundary_cells["inflow"])
+                if "inflow" in mesh.tag_boundary_cells else 0)
+    d.workload_info = info
+    return d

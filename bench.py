@@ -107,11 +107,21 @@ def build_workload(m, precision):
     return d
 
 
-def _oracle_domain(m, threads):
+def _oracle_domain(m, threads, workload="inflow_bumps", cells=1.2e6):
+    """The oracle (restated reference, OpenMP) set up with the workload's mesh,
+    initial state, boundaries and operators, after one warm-up step."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from anuga_core_gb300 import workloads
-    d = workloads.inflow_bumps(m=m)
+    if workload == "rain_polygon":
+        d = workloads.rain_polygon(target_cells=cells, precision="fp64")
+        kinds = {"inflow": ("dirichlet", (3.0, 0.0, 0.0)), "wall": ("reflective", None)}
+        rates = [(op.indices, op.rate) for op in d.fractional_step_operators]
+    else:
+        d = workloads.inflow_bumps(m=m)
+        kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+                 "top": ("reflective", None), "bottom": ("reflective", None)}
+        rates = []
     oracle.build()
     oracle.set_threads(threads)
     oracle.set_parallel_extrapolation(True)
@@ -120,9 +130,9 @@ def _oracle_domain(m, threads):
     od.set_centroid_state(Q["stage"].centroid_values, Q["xmomentum"].centroid_values,
                           Q["ymomentum"].centroid_values, Q["elevation"].centroid_values,
                           Q["friction"].centroid_values)
-    kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
-             "top": ("reflective", None), "bottom": ("reflective", None)}
     od.set_boundaries([(d.mesh.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in d.mesh.tag_boundary_cells])
+    for idx, rate in rates:
+        od.add_rate(idx, rate)
     gen = od.evolve(yieldstep=1e9, finaltime=None, max_steps=10**9)
     next(gen)                      # initial distribute
     od.relative_yieldtime = 1e300
@@ -139,13 +149,13 @@ def _oracle_steps(od, steps):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(m, steps, threads):
+def cpu_baseline(m, steps, threads, workload="inflow_bumps", cells=1.2e6):
     """Oracle (restated reference, OpenMP) on the same workload: `steps` DE1
     steps of the full mesh after one warm-up step."""
-    od, N = _oracle_domain(m, threads)
+    od, N = _oracle_domain(m, threads, workload, cells)
     el = _oracle_steps(od, steps)
     return {"value": N * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d DE1 steps of the %d-triangle inflow_bumps mesh (%.1f s)" % (steps, N, el)}
+            "sample": "%d DE1 steps of the %d-triangle %s mesh (%.1f s)" % (steps, N, workload, el)}
 
 
 def run_reference(args):
@@ -155,7 +165,7 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    od, N = _oracle_domain(args.m, threads)
+    od, N = _oracle_domain(args.m, threads, args.workload, args.cells)
     _oracle_steps(od, args.warmup)
     el = _oracle_steps(od, args.steps)
     v = N * args.steps / el
@@ -163,8 +173,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2" %
-                       (args.m, args.m, N), "cells": N, "l2": "inputs larger than L2"},
+            "config": {"workload": workload_name(args, N), "cells": N, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d DE1 steps of the full %d-triangle mesh after %d warm-up steps (%.1f s)"
                              % (args.steps, N, args.warmup, el)},
@@ -184,7 +193,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60, dest="cpu_steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=64, help="serve workload: number of requests")
-    ap.add_argument("--workload", default="inflow_bumps", choices=["inflow_bumps", "batch", "serve"],
+    ap.add_argument("--cells", type=float, default=1.2e6, help="rain_polygon workload: target triangles")
+    ap.add_argument("--workload", default="inflow_bumps", choices=["inflow_bumps", "rain_polygon", "batch", "serve"],
                     help="inflow_bumps: one 4M-triangle mesh; batch: 256 scenarios (~20M triangles) in one pool")
     ap.add_argument("--batch-count", type=int, default=256, dest="batch_count")
     args = ap.parse_args()
@@ -207,6 +217,14 @@ def main():
     if args.workload == "serve":
         return run_serve(args, torch)
     precisions = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    if args.workload == "rain_polygon":
+        from anuga_core_gb300 import workloads as W
+
+        def builder(prec):
+            return W.rain_polygon(target_cells=args.cells, precision=prec)
+    else:
+        def builder(prec):
+            return build_workload(args.m, prec)
 
     def barrier():
         if dist is not None:
@@ -217,22 +235,21 @@ def main():
     sampler.start()
     res = {}
     for prec in precisions:
-        res[prec] = measure_single(args, prec, torch, world, barrier, dist)
+        res[prec] = measure_single(args, prec, torch, world, barrier, dist, builder)
     clocks = sampler.stop()
     if rank == 0:
         head = res[precisions[-1]]
         N = head["cells"]
         cpu = None
         if not args.no_cpu and world == 1:
-            cpu = cpu_baseline(args.m, args.cpu_steps, os.cpu_count() or 1)
+            cpu = cpu_baseline(args.m, args.cpu_steps, os.cpu_count() or 1, args.workload, args.cells)
         line = {
             "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if head["precision"] == "fp64" else "f32 flux / f64 accumulate",
             "data": "synthetic",
-            "config": {"workload": "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2" %
-                       (args.m, args.m, N), "cells": N, "precision": head["precision"],
+            "config": {"workload": workload_name(args, N), "cells": N, "precision": head["precision"],
                        "l2": "inputs larger than L2 (state %.0f MB)" % (head["state_bytes"] / 1e6),
                        "parallelism": "replicas" if world > 1 else "single", "autotune": head["autotune"]},
             "roofline": head["roofline"],
@@ -263,11 +280,18 @@ KERNEL_BYTES_PER_CELL = {"mixed": {"flux": 136.0 + 208.0, "update": 100.0},
                          "fp64": {"extrap": 2 * 272.0}}
 
 
-def measure_single(args, precision, torch, world, barrier, dist):
+def workload_name(args, N):
+    if args.workload == "rain_polygon":
+        return ("rain_polygon: 20-vertex random polygon, %d triangles (Delaunay, <=50 m^2, <=12.5 m^2 in the "
+                "refined region), value-noise bed, rain 50 mm/h on 1 km^2, 3 m inflow, DE1 RK2" % N)
+    return "inflow_bumps %dx%d rectangular cross (%d triangles), DE1 RK2" % (args.m, args.m, N)
+
+
+def measure_single(args, precision, torch, world, barrier, dist, builder):
     """Device-resident throughput, per-kernel roofline and the end-to-end
     figure (host buffers through the C ABI) of one precision form."""
     from anuga_core_gb300 import _lib
-    d = build_workload(args.m, precision)
+    d = builder(precision)
     N = len(d)
     d.distribute_to_vertices_and_edges()
     scn = d._scn
@@ -315,7 +339,11 @@ def measure_single(args, precision, torch, world, barrier, dist):
         roof["traffic"] = roof["traffic"] * N
         roof["traffic_note"] = TRAFFIC_PER_STEP[(precision, dominant)]["note"]
     if precision == "fp64":
-        roof["note"] = "FP64-pipe bound (DFMA ~0.5 T/s on GB300); HBM fraction reported for reference"
+        fp = _lib.fp64_throughput()
+        roof["fp64_measured"] = fp
+        roof["note"] = ("FP64-pipe bound: the measured FP64 rates (fp64_measured, G ops/s) are 1/54 of the FP32 "
+                        "rate; ncu shows the extrapolation kernel's FP64 pipe 83%% busy at 6%% of HBM bandwidth "
+                        "(profiles/k_extrap_inflow_bumps_1M_fp64.md)")
     alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
     ach_s = alg_step / (ms_per_step / 1e3) / 1e9
     step_roof = {"achieved": ach_s, "peak": hbm, "unit": "GB/s", "frac": ach_s / hbm,

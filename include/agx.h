@@ -208,6 +208,11 @@ int32_t agx_last_error(char* buf, int32_t n);
 int32_t agx_version(void);
 /* Number of kernels this library launched since load (launch accounting). */
 int64_t agx_kernel_launches(void);
+/* FP64 throughput of the current device in G operations/s (DFMA, IEEE DDIV,
+ * IEEE DSQRT), measured with dependent chains of 8-way ILP over the whole
+ * device: the compute ceiling of the plain FP64 path.  No counterpart in the
+ * reference (measurement only); allocates and frees a small result buffer. */
+agx_status agx_fp64_throughput(double* dfma_gops, double* ddiv_gops, double* dsqrt_gops);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,31 @@ def test_delaunay_dry_start_inflow_depth_error_within_1mm(oracle_mod):
     assert err <= DEPTH_TOL, err
 
 
+def test_rain_polygon_depth_error_within_1mm(oracle_mod):
+    """The unstructured rain-and-inflow workload (random polygon, refined
+    region, value-noise bed, rain patch, inflow segment) at 20k triangles."""
+    d = workloads.rain_polygon(target_cells=2.0e4, precision="mixed")
+    op = d.fractional_step_operators[0]
+    kinds = {"inflow": ("dirichlet", (3.0, 0.0, 0.0)), "wall": ("reflective", None)}
+    Q = d.quantities
+    st = dict(stage=Q["stage"].centroid_values.copy(), xmom=Q["xmomentum"].centroid_values.copy(),
+              ymom=Q["ymomentum"].centroid_values.copy(), elevation=Q["elevation"].centroid_values.copy(),
+              friction=Q["friction"].centroid_values.copy())
+    od = make_oracle(oracle_mod, d.mesh, "DE1", st, kinds, rates=[(op.indices, op.rate)])
+    for _ in d.evolve(yieldstep=30.0, finaltime=120.0):
+        pass
+    for _ in od.evolve(yieldstep=30.0, finaltime=120.0):
+        pass
+    z = Q["elevation"].centroid_values
+    h_gpu = np.maximum(Q["stage"].centroid_values - z, 0)
+    h_ref = np.maximum(od.stage_c - od.bed_c, 0)
+    err = np.abs(h_gpu - h_ref).max()
+    assert err <= DEPTH_TOL, err
+    A = d.mesh.areas
+    vol_gpu, vol_ref = float(np.sum(h_gpu * A)), float(np.sum(h_ref * A))
+    assert abs(vol_gpu - vol_ref) <= 1e-5 * vol_ref, (vol_gpu, vol_ref)
+
+
 def test_closed_domain_conserves_volume():
     d = workloads.dam_break(m=40, flow_algorithm="DE1", precision="mixed")
     v0 = d.get_water_volume()

@@ -267,3 +267,13 @@ def test_single_triangle_and_dry_domain(oracle_mod):
         pass
     assert np.array_equal(d.quantities["stage"].centroid_values, z)
     assert d.total_steps == 1
+
+
+def test_fp64_throughput_probe():
+    """The FP64 ceiling the plain path is reported against: positive, and DFMA
+    faster than the IEEE division and square root."""
+    from anuga_core_gb300 import _lib
+    r = _lib.fp64_throughput()
+    assert 10.0 < r["dfma_gops"] < 1.0e5
+    assert 0.0 < r["ddiv_gops"] < r["dfma_gops"]
+    assert 0.0 < r["dsqrt_gops"] < r["dfma_gops"]

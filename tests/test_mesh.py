@@ -41,3 +41,19 @@ def test_inconsistent_orientation_rejected():
     e = np.array([[0, 1, 2], [1, 2, 3]])    # second triangle is clockwise -> degenerate area check
     with pytest.raises(ValueError):
         Mesh(p, e)
+
+
+def test_polygon_mesh_meets_its_area_limits():
+    from anuga_core_gb300.geometry import inside_polygon
+    from anuga_core_gb300.workloads import polygon_mesh, value_noise
+    mesh, info = polygon_mesh(2.0e4, seed=7)
+    assert abs(len(mesh) - 2.0e4) < 0.15 * 2.0e4
+    assert mesh.areas.min() > 0.0 and mesh.areas.max() <= 50.0 + 1e-9
+    inner = np.array(info["refined"])
+    fine = inside_polygon(mesh.centroid_coordinates, inner)
+    assert fine.size > 0 and mesh.areas[fine].max() <= 12.5 + 1e-9
+    assert "inflow" in mesh.tag_boundary_cells and "wall" in mesh.tag_boundary_cells
+    z = value_noise(mesh.nodes[:, 0], mesh.nodes[:, 1], seed=7)
+    assert abs(z.min() + 10.0) < 1e-9 and abs(z.max() - 30.0) < 1e-9
+    again, _ = polygon_mesh(2.0e4, seed=7)
+    assert np.array_equal(again.triangles, mesh.triangles)
