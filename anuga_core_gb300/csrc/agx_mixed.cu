@@ -424,7 +424,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
       const int nbr[3] = {cn.x, cn.y, cn.z};
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        const EdgeState L = own[i];
+        const EdgeState L = es[threadIdx.x * 3 + i];   // own edge from the staging (fewer live registers)
         const int n = nbr[i];
         float hre, uhr, vhr, dd = 0.0f;
         const float len = sqrtf(evx[i] * evx[i] + evy[i] * evy[i]);
