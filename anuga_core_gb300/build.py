@@ -32,6 +32,12 @@ UNITS = [
     ("agx_probe.cu", []),
 ]
 
+# host C++ units (g++, OpenMP): the native mesh and table builders
+HOST_UNITS = [
+    ("agx_mesh.cpp", []),
+]
+HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-I" + INCLUDE, "-I" + CSRC]
+
 
 def nvcc():
     exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
@@ -47,10 +53,19 @@ def _sources():
 def _deps():
     out = []
     for fn in os.listdir(CSRC):
-        if fn.endswith((".cu", ".cuh", ".h")):
+        if fn.endswith((".cu", ".cuh", ".h", ".cpp")):
             out.append(os.path.join(CSRC, fn))
-    out.append(os.path.join(INCLUDE, "agx.h"))
+    for fn in os.listdir(INCLUDE):
+        if fn.endswith(".h"):
+            out.append(os.path.join(INCLUDE, fn))
     return out
+
+
+def cxx():
+    exe = shutil.which("g++") or shutil.which("c++")
+    if not exe:
+        raise RuntimeError("g++ not found: a C++17 compiler is required to build libagx")
+    return exe
 
 
 def needs_build():
@@ -74,12 +89,18 @@ def build(force=False, verbose=False, ptxas_info=False):
         if ptxas_info:
             cmd += ["-Xptxas", "-v"]
         jobs.append((cmd, obj))
+    for name, flags in HOST_UNITS:
+        src = os.path.join(CSRC, name)
+        if not os.path.exists(src):
+            continue
+        obj = os.path.join(objdir, name + ".o")
+        jobs.append(([cxx()] + HOST_FLAGS + flags + ["-c", src, "-o", obj], obj))
 
     def run(job):
         cmd, obj = job
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+            raise RuntimeError("compile failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         return r.stderr
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
@@ -88,7 +109,7 @@ def build(force=False, verbose=False, ptxas_info=False):
         for lg in logs:
             sys.stderr.write(lg)
     tmp = LIB + ".tmp"
-    cmd = [exe] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs]
+    cmd = [exe] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + [o for _, o in jobs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)

@@ -12,9 +12,11 @@ bit-identical:
   (neighbours, neighbour edges, number of boundaries, surrogate neighbours,
   boundary dictionary and enumeration).
 
-Neighbour matching is vectorised (sort + binary search over directed edge
-keys) instead of the reference's C++ hash table
-(``neighbour_table.cpp``); the result is identical.
+Geometry and neighbours are computed by the native builder
+(``csrc/agx_mesh.cpp``: directed edges bucketed by their first vertex instead
+of the reference's hash table in ``neighbour_table.cpp``; the result is
+identical).  ``_geometry_numpy`` / ``_neighbours_numpy`` restate the same in
+numpy for the tests.
 """
 from __future__ import annotations
 
@@ -97,8 +99,33 @@ class Mesh:
     def __len__(self):
         return self.number_of_triangles
 
-    # general_mesh.py:134-267
+    # general_mesh.py:134-267 (native: agx_mesh_geometry)
     def _geometry(self):
+        from . import native
+        g, bad = native.mesh_geometry(self.nodes, self.triangles, self.use_inscribed_circle)
+        self.vertex_coordinates = g["V"]
+        self.edge_midpoint_coordinates = g["E"]
+        self.areas = g["areas"]
+        if bad >= 0:
+            raise ValueError("Degenerate Triangle(s) %s" % np.where(self.areas <= 0.0)[0][:20])
+        self.normals = g["normals"]
+        self.edgelengths = g["lengths"]
+        self.centroid_coordinates = g["C"]
+        self.radii = g["radii"]
+
+    # neighbour_table.cpp + neighbour_mesh.py:296-346 (native: agx_mesh_neighbours)
+    def _neighbours(self):
+        from . import native
+        N = self.number_of_triangles
+        nb, ne, nbnd = native.mesh_neighbours(self.number_of_nodes, self.triangles)
+        self.neighbours = nb
+        self.neighbour_edges = ne
+        self.number_of_boundaries = nbnd
+        rng = np.arange(N, dtype=np.int64)[:, None]
+        self.surrogate_neighbours = np.where(self.neighbours < 0, rng, self.neighbours)
+
+    # numpy restatement of _geometry (the reference the native builder is tested against)
+    def _geometry_numpy(self):
         N = self.number_of_triangles
         tri = self.triangles
         V = np.zeros((3 * N, 2), dtype=float)
@@ -153,8 +180,8 @@ class Mesh:
             c = np.sqrt((x2 - x0) ** 2 + (y2 - y0) ** 2)
             self.radii = 2.0 * self.areas / (a + b + c)
 
-    # neighbour_table.cpp + neighbour_mesh.py:296-346
-    def _neighbours(self):
+    # numpy restatement of _neighbours (the reference the native builder is tested against)
+    def _neighbours_numpy(self):
         N = self.number_of_triangles
         tri = self.triangles
         M = np.int64(max(self.number_of_nodes, 1))

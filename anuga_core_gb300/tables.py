@@ -19,8 +19,10 @@ import numpy as np
 GEO_STRIDE = 11
 
 
-def pack_tables(mesh, tri_full_flag=None, per_side_edges=None, order=None):
-    """Return a dict of numpy arrays for ``agx_scenario_create``.
+def pack_tables_numpy(mesh, tri_full_flag=None, per_side_edges=None, order=None):
+    """numpy restatement of :func:`pack_tables` (the tests' reference).
+
+    Return a dict of numpy arrays for ``agx_scenario_create``.
 
     per_side_edges: optional bool [N,3] forcing per-side evaluation of slots
     (used for low-Froude scaling and riverwalls, where the edge flux is not
@@ -135,7 +137,7 @@ def pack_tables(mesh, tri_full_flag=None, per_side_edges=None, order=None):
                 vertex_coordinates=np.ascontiguousarray(np.asarray(mesh.vertex_coordinates, np.float64).ravel()))
 
 
-def morton_order(points, bits=16):
+def morton_order_numpy(points, bits=16):
     """Cell order along a Morton (Z-order) curve of the centroids, so that
     tiles of consecutive cells are compact patches of the mesh."""
     P = np.asarray(points, np.float64)
@@ -154,7 +156,7 @@ def morton_order(points, bits=16):
     return np.argsort(key, kind="stable")
 
 
-def pack_mixed(mesh, order=None):
+def pack_mixed_numpy(mesh, order=None):
     """FP32 tables of the mixed-precision form, cells in Morton order.
 
     Returns conn int32 [N,4] (neighbours in the stored order, boundary edges as
@@ -179,7 +181,7 @@ def pack_mixed(mesh, order=None):
         raise NotImplementedError("the mixed-precision form needs surrogate neighbours equal to the "
                                   "flux neighbours (no internal boundary segments)")
     if order is None:
-        order, _name, _costs = best_order(mesh)
+        order, _name, _costs = best_order_numpy(mesh)
     order = np.asarray(order, np.int64)
     inv = np.empty(N, np.int64)
     inv[order] = np.arange(N)
@@ -236,7 +238,7 @@ def pack_mixed(mesh, order=None):
     conn[:, 3] = meta
     bcell = inv[np.asarray(mesh.boundary_cells, np.int64)]
     conn_s = np.ascontiguousarray(conn[order].astype(np.int32))
-    lnk, hoff, hcnt, hcells = tile_halos(conn_s)
+    lnk, hoff, hcnt, hcells = tile_halos_numpy(conn_s)
     return dict(conn=conn_s, lnk=lnk, halo_off=hoff, halo_cnt=hcnt, halo_cells=hcells,
                 geo=np.ascontiguousarray(geo[order]),
                 area=np.ascontiguousarray(np.asarray(mesh.areas, np.float64)[order]),
@@ -249,7 +251,7 @@ HALO_MAX = 256          # halo cells a tile can stage in shared memory
 LNK_INLINE = 1023       # local index meaning "reconstruct this neighbour inline"
 
 
-def tile_halos(conn, tile=TILE, halo_max=HALO_MAX):
+def tile_halos_numpy(conn, tile=TILE, halo_max=HALO_MAX):
     """Per tile of `tile` consecutive cells: the outside cells whose edges the
     tile's fluxes need (its halo), and for every cell slot the local index of
     the neighbour in the tile's staging area (own cells 0..tile-1, halo cells
@@ -290,7 +292,7 @@ def tile_halos(conn, tile=TILE, halo_max=HALO_MAX):
     return (lnk.astype(np.int32), off2.astype(np.int32), cnt_clamped.astype(np.int32), hc.astype(np.int32))
 
 
-def hilbert_order(points, bits=16):
+def hilbert_order_numpy(points, bits=16):
     """Cell order along a Hilbert curve of the centroids (better locality
     than Morton: consecutive cells are always adjacent patches)."""
     P = np.asarray(points, np.float64)
@@ -315,7 +317,7 @@ def hilbert_order(points, bits=16):
     return np.argsort(d, kind="stable")
 
 
-def halo_cost(mesh, order, tile=TILE):
+def halo_cost_numpy(mesh, order, tile=TILE):
     """Fraction of extra reconstructions (halo cells per own cell) of an order."""
     N = len(mesh)
     inv = np.empty(N, np.int64)
@@ -328,6 +330,90 @@ def halo_cost(mesh, order, tile=TILE):
     return pairs.size / max(N, 1)
 
 
+def best_order_numpy(mesh, tile=TILE):
+    """numpy restatement of :func:`best_order`."""
+    C = mesh.centroid_coordinates
+    cands = {"hilbert": hilbert_order_numpy(C), "morton": morton_order_numpy(C)}
+    costs = {k: halo_cost_numpy(mesh, v, tile) for k, v in cands.items()}
+    name = min(costs, key=costs.get)
+    return cands[name], name, costs
+
+
+# ---------------------------------------------------------------------------
+# Native builders (csrc/agx_mesh.cpp): the product path.  Each computes the
+# same bits as its *_numpy restatement above.
+
+def pack_tables(mesh, tri_full_flag=None, per_side_edges=None, order=None):
+    """Return a dict of numpy arrays for ``agx_scenario_create``.
+
+    per_side_edges: optional bool [N,3] forcing per-side evaluation of slots
+    (used for low-Froude scaling and riverwalls, where the edge flux is not
+    antisymmetric).  order: original index of each cell (for the ordering
+    bits); defaults to the identity.
+    """
+    from . import native
+    N = len(mesh)
+    if N >= (1 << 29):
+        raise ValueError("mesh too large for 32-bit slot indices")
+    normals = np.asarray(mesh.normals, np.float64)
+    lengths = np.asarray(mesh.edgelengths, np.float64)
+    conn, surr, geo, edge_slot, edge_opp = native.pack_plain(
+        N, mesh.neighbours, mesh.neighbour_edges, mesh.surrogate_neighbours, mesh.number_of_boundaries,
+        tri_full_flag, per_side_edges, order, normals, lengths, mesh.centroid_coordinates,
+        mesh.edge_midpoint_coordinates)
+    inv_area = 1.0 / np.asarray(mesh.areas, np.float64)
+    bslot = (3 * np.asarray(mesh.boundary_cells, np.int64) + np.asarray(mesh.boundary_edges, np.int64)).astype(np.int32)
+    return dict(conn=conn, surr=surr, geo=geo, edge_slot=edge_slot, edge_opp=edge_opp,
+                normals=np.ascontiguousarray(normals.ravel()), edgelengths=np.ascontiguousarray(lengths.ravel()),
+                radii=np.ascontiguousarray(np.asarray(mesh.radii, np.float64)),
+                areas=np.ascontiguousarray(np.asarray(mesh.areas, np.float64)),
+                inv_area=np.ascontiguousarray(inv_area), boundary_slot=np.ascontiguousarray(bslot),
+                vertex_coordinates=np.ascontiguousarray(np.asarray(mesh.vertex_coordinates, np.float64).ravel()))
+
+
+def morton_order(points, bits=16):
+    """Cell order along a Morton (Z-order) curve of the centroids, so that
+    tiles of consecutive cells are compact patches of the mesh."""
+    from . import native
+    return native.sfc_order(points, "morton", bits)
+
+
+def hilbert_order(points, bits=16):
+    """Cell order along a Hilbert curve of the centroids (better locality
+    than Morton: consecutive cells are always adjacent patches)."""
+    from . import native
+    return native.sfc_order(points, "hilbert", bits)
+
+
+def tile_halos(conn, tile=TILE, halo_max=HALO_MAX):
+    """Per tile of `tile` consecutive cells: the outside cells whose edges the
+    tile's fluxes need (its halo), and for every cell slot the local index of
+    the neighbour in the tile's staging area (own cells 0..tile-1, halo cells
+    tile..tile+H-1, boundary edges LNK_INLINE, packed 10 bits per slot).
+
+    Returns (lnk int32 [N], halo_off int32 [T], halo_cnt int32 [T],
+    halo_cells int32 [sum H])."""
+    from . import native
+    lnk, off, cnt, hc, _unclamped = native.tile_halos(conn, tile, halo_max, LNK_INLINE)
+    return lnk, off, cnt, hc
+
+
+def _stored_conn(mesh, order):
+    N = len(mesh)
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    nb = np.asarray(mesh.neighbours, np.int64)[order]
+    conn = np.zeros((N, 4), np.int32)
+    conn[:, :3] = np.where(nb >= 0, inv[np.where(nb >= 0, nb, 0)], -1)
+    return conn
+
+
+def halo_cost(mesh, order, tile=TILE):
+    """Fraction of extra reconstructions (halo cells per own cell) of an order."""
+    from . import native
+    return native.tile_halos(_stored_conn(mesh, order), tile, HALO_MAX, LNK_INLINE, count_only=True) / max(len(mesh), 1)
+
+
 def best_order(mesh, tile=TILE):
     """The cheaper of the Morton and Hilbert orders by halo cost (the
     reordering choice of the autotuner); returns (order, name, costs)."""
@@ -336,3 +422,30 @@ def best_order(mesh, tile=TILE):
     costs = {k: halo_cost(mesh, v, tile) for k, v in cands.items()}
     name = min(costs, key=costs.get)
     return cands[name], name, costs
+
+
+def pack_mixed(mesh, order=None):
+    """FP32 tables of the mixed-precision form, cells in a space-filling-curve
+    order (see :func:`pack_mixed_numpy` for the layout; same arrays, built by
+    the native builder)."""
+    from . import native
+    N = len(mesh)
+    nb = np.asarray(mesh.neighbours, np.int64)
+    sn = np.asarray(mesh.surrogate_neighbours, np.int64)
+    cells = np.arange(N, dtype=np.int64)
+    expected = np.where(nb >= 0, nb, cells[:, None])
+    if not np.array_equal(expected, sn):
+        raise NotImplementedError("the mixed-precision form needs surrogate neighbours equal to the "
+                                  "flux neighbours (no internal boundary segments)")
+    if order is None:
+        order, _name, _costs = best_order(mesh)
+    order = np.asarray(order, np.int64)
+    conn_s, geo, area_s, order_s = native.pack_mixed(
+        order, nb, mesh.neighbour_edges, sn, mesh.number_of_boundaries, mesh.centroid_coordinates,
+        mesh.edge_midpoint_coordinates, mesh.vertex_coordinates, mesh.radii, mesh.areas)
+    inv = np.empty(N, np.int64)
+    inv[order] = np.arange(N)
+    bcell = inv[np.asarray(mesh.boundary_cells, np.int64)]
+    lnk, hoff, hcnt, hcells = tile_halos(conn_s)
+    return dict(conn=conn_s, lnk=lnk, halo_off=hoff, halo_cnt=hcnt, halo_cells=hcells, geo=geo, area=area_s,
+                order=order_s, boundary_cell=np.ascontiguousarray(bcell.astype(np.int32)))

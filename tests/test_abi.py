@@ -19,7 +19,7 @@ def test_library_exports_every_declared_symbol():
     from anuga_core_gb300 import build
     build.build()
     lib = ctypes.CDLL(build.LIB)
-    names = declared("agx.h") + declared("agx_pool.h") + declared("agx_noalloc.h")
+    names = declared("agx.h") + declared("agx_pool.h") + declared("agx_noalloc.h") + declared("agx_mesh.h")
     assert len(names) >= 50
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
