@@ -35,7 +35,9 @@ def test_oracle_phases_bit_exact(golden, oracle_mod, alg):
         assert np.array_equal(getattr(od, a + "_b"), f["bc.%s.boundary_values" % q])
     assert od.compute_fluxes(0) == float(f["flux.flux_timestep"])
     assert np.array_equal(od.max_speed, f["flux.max_speed"])
-    assert np.array_equal(od.boundary_flux_sum, f["flux.boundary_flux_sum"])
+    # an OpenMP sum in both the reference and the oracle: its last place
+    # follows the host's thread count
+    np.testing.assert_allclose(od.boundary_flux_sum, f["flux.boundary_flux_sum"], rtol=1e-13, atol=0)
     for q, a in [("stage", "stage"), ("xmomentum", "xmom"), ("ymomentum", "ymom")]:
         assert np.array_equal(getattr(od, a + "_x"), f["flux.%s.explicit_update" % q])
     od.compute_forcing_terms()
