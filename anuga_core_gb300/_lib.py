@@ -90,6 +90,8 @@ def load(path=None):
         "agx_set_field": ([H, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_get_field": ([H, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_device_ptr": ([H, ctypes.c_int32, P(ctypes.c_void_p), P(ctypes.c_int64)], ctypes.c_int32),
+        "agx_set_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
+        "agx_get_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary": ([H, _i32p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary_series": ([H, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_add_rate_operator": ([H, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
@@ -215,6 +217,16 @@ class Scenario:
         a = np.empty(n, np.float64) if out is None else out
         check(self.L.agx_get_field(self.h, FIELD[name], ptr_f64(a), n))
         return a
+
+    def set_state(self, w, uh, vh):
+        """stage, xmomentum, ymomentum centroid values in one call."""
+        a = [np.ascontiguousarray(np.asarray(x, np.float64).ravel()) for x in (w, uh, vh)]
+        check(self.L.agx_set_state(self.h, ptr_f64(a[0]), ptr_f64(a[1]), ptr_f64(a[2]), a[0].size))
+
+    def get_state(self, w=None, uh=None, vh=None):
+        out = [np.empty(self.N) if x is None else x for x in (w, uh, vh)]
+        check(self.L.agx_get_state(self.h, ptr_f64(out[0]), ptr_f64(out[1]), ptr_f64(out[2]), self.N))
+        return out
 
     def device_ptr(self, name):
         p = ctypes.c_void_p()

@@ -348,6 +348,28 @@ agx_status agx_get_field(agx_handle h, int32_t f, double* host, int64_t n) {
   return sync(h);
 }
 
+// The conserved centroid state (stage, xmomentum, ymomentum) in one call:
+// three copies on the scenario's stream and one synchronisation.
+agx_status agx_set_state(agx_handle h, const double* w, const double* uh, const double* vh, int64_t n) {
+  if (!h || !w || !uh || !vh) return fail(AGX_E_INVALID, "bad arguments");
+  if (n != h->N) return fail(AGX_E_INVALID, "the state has %d cells, got %lld", h->N, (long long)n);
+  if (n == 0) return AGX_OK;
+  CK(cudaMemcpyAsync(h->field[AGX_STAGE_C], w, (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->field[AGX_XMOM_C], uh, (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->field[AGX_YMOM_C], vh, (size_t)n * 8, cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+agx_status agx_get_state(agx_handle h, double* w, double* uh, double* vh, int64_t n) {
+  if (!h || !w || !uh || !vh) return fail(AGX_E_INVALID, "bad arguments");
+  if (n != h->N) return fail(AGX_E_INVALID, "the state has %d cells, asked for %lld", h->N, (long long)n);
+  if (n == 0) return AGX_OK;
+  CK(cudaMemcpyAsync(w, h->field[AGX_STAGE_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(uh, h->field[AGX_XMOM_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(vh, h->field[AGX_YMOM_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
 agx_status agx_device_ptr(agx_handle h, int32_t f, void** ptr, int64_t* n) {
   if (!h || f < 0 || f >= AGX_FIELD_COUNT || !ptr) return fail(AGX_E_INVALID, "bad handle or field");
   *ptr = h->field[f];

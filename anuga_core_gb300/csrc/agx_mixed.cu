@@ -1323,6 +1323,61 @@ agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t f, const double* 
   return psync(p);
 }
 
+__global__ void k_gather3(double* w, double* uh, double* vh, const double* src, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const int o = order[j];
+    w[j] = src[o];
+    uh[j] = src[(size_t)n + o];
+    vh[j] = src[2 * (size_t)n + o];
+  }
+}
+__global__ void k_scatter3(double* dst, const double* w, const double* uh, const double* vh, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const int o = order[j];
+    dst[o] = w[j];
+    dst[(size_t)n + o] = uh[j];
+    dst[2 * (size_t)n + o] = vh[j];
+  }
+}
+
+// The conserved state (stage, xmomentum, ymomentum) in the caller's cell
+// order, in one call: three copies through the staging buffer, one
+// permutation kernel, one synchronisation.
+agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const double* uh, const double* vh, int64_t n) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !w || !uh || !vh)
+    return pfail(AGX_E_INVALID, "bad arguments");
+  ScnHost& sh = p->scn[sid];
+  if (n != sh.N) return pfail(AGX_E_INVALID, "the state has %d cells", sh.N);
+  const int c0 = sh.tile0 * TILE;
+  cudaStream_t st = p->stream;
+  PCK(cudaMemcpyAsync(p->staging, w, n * 8, cudaMemcpyHostToDevice, st));
+  PCK(cudaMemcpyAsync(p->staging + n, uh, n * 8, cudaMemcpyHostToDevice, st));
+  PCK(cudaMemcpyAsync(p->staging + 2 * n, vh, n * 8, cudaMemcpyHostToDevice, st));
+  k_gather3<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->staging, sh.order, (int)n);
+  count_launch();
+  PCK(cudaGetLastError());
+  sh.work_dirty = true;
+  return psync(p);
+}
+
+agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, double* vh, int64_t n) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !w || !uh || !vh)
+    return pfail(AGX_E_INVALID, "bad arguments");
+  ScnHost& sh = p->scn[sid];
+  if (n != sh.N) return pfail(AGX_E_INVALID, "the state has %d cells", sh.N);
+  const int c0 = sh.tile0 * TILE;
+  cudaStream_t st = p->stream;
+  k_scatter3<<<nblk1((int)n), 256, 0, st>>>(p->staging, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, sh.order, (int)n);
+  count_launch();
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(w, p->staging, n * 8, cudaMemcpyDeviceToHost, st));
+  PCK(cudaMemcpyAsync(uh, p->staging + n, n * 8, cudaMemcpyDeviceToHost, st));
+  PCK(cudaMemcpyAsync(vh, p->staging + 2 * n, n * 8, cudaMemcpyDeviceToHost, st));
+  return psync(p);
+}
+
 agx_status agx_pool_get_field(agx_pool p, int32_t sid, int32_t f, double* host, int64_t n) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
   ScnHost& sh = p->scn[sid];

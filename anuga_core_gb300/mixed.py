@@ -33,6 +33,8 @@ def lib():
             "agx_pool_footprint": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int32], ctypes.c_int64),
             "agx_pool_bytes_per_cell": ([], ctypes.c_int64),
             "agx_pool_set_stream": ([H, ctypes.c_void_p], ctypes.c_int32),
+            "agx_pool_set_state": ([H, ctypes.c_int32, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
+            "agx_pool_get_state": ([H, ctypes.c_int32, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
             "agx_pool_add": ([H, ctypes.c_int64, ctypes.c_int64, _i32p, _f32p, _f64p, _i32p, _i32p, _i32p,
                               _i32p, _i32p, ctypes.c_int64, _i32p, P(_lib.Params), P(ctypes.c_int32)],
                              ctypes.c_int32),
@@ -140,6 +142,17 @@ class Pool:
     def set_field(self, sid, name, values):
         a = np.ascontiguousarray(np.asarray(values, np.float64).ravel())
         check(self.L.agx_pool_set_field(self.h, sid, _lib.FIELD[name], a.ctypes.data_as(_f64p), a.size))
+
+    def set_state(self, sid, w, uh, vh):
+        """stage, xmomentum, ymomentum centroid values of one scenario in one call."""
+        a = [np.ascontiguousarray(np.asarray(x, np.float64).ravel()) for x in (w, uh, vh)]
+        check(self.L.agx_pool_set_state(self.h, sid, *[x.ctypes.data_as(_f64p) for x in a], a[0].size))
+
+    def get_state(self, sid, w=None, uh=None, vh=None):
+        N, _ = self._keep[sid]
+        out = [np.empty(N) if x is None else x for x in (w, uh, vh)]
+        check(self.L.agx_pool_get_state(self.h, sid, *[x.ctypes.data_as(_f64p) for x in out], N))
+        return out
 
     def get_field(self, sid, name, out=None):
         N, _ = self._keep[sid]
@@ -262,6 +275,12 @@ class MixedScenario:
     def set(self, name, values):
         if name in self.CENTROID_IN:
             self.pool.set_field(self.sid, name, values)
+
+    def set_state(self, w, uh, vh):
+        self.pool.set_state(self.sid, w, uh, vh)
+
+    def get_state(self, w=None, uh=None, vh=None):
+        return self.pool.get_state(self.sid, w, uh, vh)
 
     def get(self, name, out=None):
         n = self.field_len(name)

@@ -137,6 +137,11 @@ agx_status agx_set_field(agx_handle h, int32_t field, const double* host, int64_
 agx_status agx_get_field(agx_handle h, int32_t field, double* host, int64_t n);
 /* Device address of a field (for zero-copy torch views).  Valid until destroy. */
 agx_status agx_device_ptr(agx_handle h, int32_t field, void** ptr, int64_t* n);
+/* The conserved centroid state (stage, xmomentum, ymomentum; N values each)
+ * in one call with one synchronisation: the per-yield exchange of
+ * Domain.get_conserved_quantities / set_quantity (quantity.py:709-1055). */
+agx_status agx_set_state(agx_handle h, const double* w, const double* uh, const double* vh, int64_t n);
+agx_status agx_get_state(agx_handle h, double* w, double* uh, double* vh, int64_t n);
 
 /* Bind boundary conditions: kind[B] and values[B*3] (w, uh, vh) for
  * Dirichlet.  Domain.set_boundary + update_boundary (generic_domain.py:2288-2306). */

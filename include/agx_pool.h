@@ -54,6 +54,11 @@ agx_status agx_pool_capacity(agx_pool p, int64_t* free_cells, int64_t* free_boun
 agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t field, const double* host, int64_t n);
 agx_status agx_pool_get_field(agx_pool p, int32_t sid, int32_t field, double* host, int64_t n);
 
+/* The conserved state (stage, xmomentum, ymomentum; N values each) in one
+ * call with one synchronisation. */
+agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const double* uh, const double* vh, int64_t n);
+agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, double* vh, int64_t n);
+
 /* Boundary conditions (Domain.set_boundary, generic_domain.py:2288-2306). */
 agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, const double* values, int64_t B);
 agx_status agx_pool_set_boundary_series(agx_pool p, int32_t sid, const double* rows, int64_t n_rows);

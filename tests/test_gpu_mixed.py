@@ -178,3 +178,18 @@ def test_snapshot_restore_and_autotune_leave_state_unchanged():
         outs.append(d3.quantities["stage"].centroid_values.copy())
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+def test_state_exchange_in_one_call_matches_per_field():
+    d = workloads.dam_break(m=30, flow_algorithm="DE1", precision="mixed")
+    for _ in d.evolve(yieldstep=0.5, finaltime=0.5):
+        pass
+    scn = d._scn
+    w, uh, vh = scn.get_state()
+    assert np.array_equal(w, scn.get("stage_c")) and np.array_equal(uh, scn.get("xmom_c"))
+    assert np.array_equal(vh, scn.get("ymom_c"))
+    rng = np.random.default_rng(3)
+    w2, uh2, vh2 = w + 0.01 * rng.uniform(size=w.size), uh * 0.5, vh * 0.25
+    scn.set_state(w2, uh2, vh2)
+    for name, ref in (("stage_c", w2), ("xmom_c", uh2), ("ymom_c", vh2)):
+        assert np.array_equal(scn.get(name), ref), name

@@ -277,3 +277,15 @@ def test_fp64_throughput_probe():
     assert 10.0 < r["dfma_gops"] < 1.0e5
     assert 0.0 < r["ddiv_gops"] < r["dfma_gops"]
     assert 0.0 < r["dsqrt_gops"] < r["dfma_gops"]
+
+
+def test_state_exchange_in_one_call_matches_per_field():
+    from anuga_core_gb300 import workloads
+    d = workloads.dam_break(m=20)
+    for _ in d.evolve(yieldstep=0.5, finaltime=0.5):
+        pass
+    scn = d._scn
+    w, uh, vh = scn.get_state()
+    assert np.array_equal(w, scn.get("stage_c")) and np.array_equal(vh, scn.get("ymom_c"))
+    scn.set_state(w * 1.001, uh, vh * 0.5)
+    assert np.array_equal(scn.get("stage_c"), w * 1.001) and np.array_equal(scn.get("ymom_c"), vh * 0.5)
