@@ -15,8 +15,8 @@ from .mesh import Mesh, rectangular_cross
 from .domain import Domain, rectangular_cross_domain
 from .boundaries import (Reflective_boundary, Transmissive_boundary, Dirichlet_boundary, Time_boundary,
                          Transmissive_n_momentum_zero_t_momentum_set_stage_boundary)
-from .operators import Rate_operator
+from .operators import Inlet_operator, Rate_operator
 
 __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "Reflective_boundary",
            "Transmissive_boundary", "Dirichlet_boundary", "Time_boundary",
-           "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Rate_operator"]
+           "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Rate_operator", "Inlet_operator"]

@@ -96,6 +96,9 @@ def load(path=None):
         "agx_set_boundary_series": ([H, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_add_rate_operator": ([H, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
         "agx_clear_operators": ([H], ctypes.c_int32),
+        "agx_apply_operator": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
+        "agx_add_inlet_operator": ([H, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                    ctypes.c_double, ctypes.c_double], ctypes.c_int32),
         "agx_operator_influx": ([H, ctypes.c_int32, _f64p], ctypes.c_int32),
         "agx_protect": ([H, _f64p], ctypes.c_int32),
         "agx_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
@@ -252,6 +255,14 @@ class Scenario:
 
     def clear_operators(self):
         check(self.L.agx_clear_operators(self.h))
+
+    def add_inlet(self, indices, Q, area, flags=0, velocity=(0.0, 0.0)):
+        idx = np.ascontiguousarray(indices, np.int32)
+        check(self.L.agx_add_inlet_operator(self.h, ptr_i32(idx), idx.size, float(Q), float(area), int(flags),
+                                            float(velocity[0]), float(velocity[1])))
+
+    def apply_operator(self, op, rate, factor, timestep):
+        check(self.L.agx_apply_operator(self.h, int(op), float(rate), float(factor), float(timestep)))
 
     def operator_influx(self, op):
         v = ctypes.c_double()

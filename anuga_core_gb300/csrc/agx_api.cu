@@ -423,6 +423,34 @@ agx_status agx_add_rate_operator(agx_handle h, const int32_t* indices, int64_t n
   return sync(h);
 }
 
+agx_status agx_add_inlet_operator(agx_handle h, const int32_t* indices, int64_t n, double Q, double area,
+                                  int32_t flags, double velocity_u, double velocity_v) {
+  if (!h || !indices || n <= 0) return fail(AGX_E_INVALID, "an inlet needs at least one cell");
+  if (n > INLET_MAX) return fail(AGX_E_INVALID, "an inlet region holds at most %d cells, got %lld", INLET_MAX, (long long)n);
+  if (!(area > 0.0)) return fail(AGX_E_INVALID, "inlet area must be positive");
+  if ((int)h->ops.size() >= MAX_OPS) return fail(AGX_E_INVALID, "at most %d operators", MAX_OPS);
+  for (int64_t i = 0; i < n; i++)
+    if (indices[i] < 0 || indices[i] >= h->N) return fail(AGX_E_INVALID, "inlet index %d out of range", indices[i]);
+  RateOp op{nullptr, (int)n, Q, 1.0};
+  op.kind = 1;
+  op.flags = flags;
+  op.vu = velocity_u;
+  op.vv = velocity_v;
+  op.area = area;
+  CK(cudaMalloc(&op.idx, (size_t)n * 4));
+  CK(cudaMemcpyAsync(op.idx, indices, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+  h->ops.push_back(op);
+  h->graph_valid = false;
+  return sync(h);
+}
+
+agx_status agx_apply_operator(agx_handle h, int32_t op, double rate, double factor, double timestep) {
+  if (!h || op < 0 || op >= (int)h->ops.size() || !(timestep >= 0.0))
+    return fail(AGX_E_INVALID, "bad operator %d or timestep", op);
+  CK(enqueue_rate_once(h, h->stream, op, rate, factor, timestep));
+  return sync(h);
+}
+
 agx_status agx_clear_operators(agx_handle h) {
   if (!h) return fail(AGX_E_INVALID, "null handle");
   agx_status st = sync(h);

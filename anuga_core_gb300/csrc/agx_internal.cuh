@@ -100,11 +100,18 @@ __host__ __device__ inline int clock_logic(Clock* c) {
   return reason;
 }
 
+// A fractional-step operator: Rate_operator (kind 0) or Inlet_operator
+// (kind 1: rate = constant discharge Q, vu/vv the imposed velocity when
+// flags & 1, zero velocity when flags & 2, area = the inlet's total area).
 struct RateOp {
   int* idx;        // device indices (nullptr: all cells)
   int n;
   double rate, factor;
+  int kind = 0;
+  int flags = 0;
+  double vu = 0.0, vv = 0.0, area = 0.0;
 };
+constexpr int INLET_MAX = 2048;     // cells of one inlet region (one block sorts them)
 
 // Everything a kernel needs, passed by value.
 struct Dev {
@@ -176,6 +183,8 @@ void end_phase_timer(double* ms, int reps, cudaEvent_t start, int abort);
 // implemented in agx_plain.cu
 cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_handle, bool set_cond);
 cudaError_t enqueue_distribute(Scenario* s, cudaStream_t st, bool with_protect, bool vertices);
+cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
+cudaError_t enqueue_op(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
 cudaError_t enqueue_protect(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_boundary(Scenario* s, cudaStream_t st, double t_override, bool stage2);
 cudaError_t enqueue_fluxes(Scenario* s, cudaStream_t st, int substep);

@@ -314,12 +314,14 @@ __global__ void k_saxpy(Dev d, double a, double b) {
 }
 
 // Rate_operator with a constant non-negative or negative rate.
-__global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor, int op) {
+// dt_arg < 0: the step's timestep from the device clock (the step loop);
+// otherwise the timestep the host gives (operators applied from the host).
+__global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor, int op, double dt_arg) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   double influx = 0.0;
   if (j < n) {
     const int k = idx ? idx[j] : j;
-    const double dt = d.clock->timestep;
+    const double dt = dt_arg >= 0.0 ? dt_arg : d.clock->timestep;
     if (rate >= 0.0) {
       const double local = factor * dt * rate;
       d.w[k] = d.w[k] + local;
@@ -339,6 +341,187 @@ __global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor,
     const double s = block_sum(influx);
     if (threadIdx.x == 0 && op < MAX_OPS) atomicAdd(&d.clock->op_influx[op], s);
   }
+}
+
+// Inlet_operator (structures/inlet_operator.py:75-165, inlet.py:107-226):
+// one block of 1024 threads for an inlet of n <= INLET_MAX cells.  The
+// discharge is Q = 0.5 (q1 + q2) over the timestep (dt_arg < 0: the step's
+// timestep from the clock).  A positive volume fills the lowest cells first
+// to a level surface (stages sorted, cumulative areas and volumes); a
+// negative one lowers all cells to one depth, or empties them.  Momenta are
+// depth x the cells' previous velocity (or the imposed one, or zero).
+constexpr int INLET_TPB = 1024;
+constexpr int INLET_PER = INLET_MAX / INLET_TPB;
+
+__device__ double inlet_block_sum(double x, double* part) {
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) part[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    double r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    r = warp_sum(r);
+    if (lane == 0) part[0] = r;
+  }
+  __syncthreads();
+  const double r = part[0];
+  __syncthreads();
+  return r;
+}
+
+// Exclusive prefix sum of v[0..INLET_MAX) in place (INLET_PER consecutive
+// values per thread, then a scan of the per-thread totals).
+__device__ void inlet_exclusive_scan(double* v, double* part) {
+  const int t = threadIdx.x;
+  double run = 0.0;
+  double loc[INLET_PER];
+#pragma unroll
+  for (int j = 0; j < INLET_PER; j++) {
+    loc[j] = run;
+    run += v[t * INLET_PER + j];
+  }
+  // inclusive scan of the thread totals across the block
+  double x = run;
+  const int lane = t & 31, wid = t >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const double y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) part[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    double w = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    part[lane] = w;
+  }
+  __syncthreads();
+  const double before = (wid > 0 ? part[wid - 1] : 0.0) + (x - run);
+#pragma unroll
+  for (int j = 0; j < INLET_PER; j++) v[t * INLET_PER + j] = before + loc[j];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(INLET_TPB) k_inlet(Dev d, RateOp op, int slot, double q1, double q2, double dt_arg) {
+  __shared__ double key[INLET_MAX];     // stages, sorted
+  __shared__ int pos[INLET_MAX];        // inlet position of each sorted stage
+  __shared__ double acc[INLET_MAX];     // cumulative areas / volumes
+  __shared__ double part[INLET_TPB / 32];
+  __shared__ int last;
+  const int n = op.n, t = threadIdx.x;
+  const double dt = dt_arg >= 0.0 ? dt_arg : d.clock->timestep;
+  const double volume = 0.5 * (q1 + q2) * dt;
+  double u[INLET_PER], v[INLET_PER], cur = 0.0;
+#pragma unroll
+  for (int j = 0; j < INLET_PER; j++) {
+    const int a = t + j * INLET_TPB;
+    u[j] = v[j] = 0.0;
+    if (a < n) {
+      const int k = op.idx[a];
+      const double h = d.w[k] - d.z[k];
+      cur += h * d.areas[k];
+      u[j] = d.uh[k] * h / (h * h + 1.0e-6);
+      v[j] = d.vh[k] * h / (h * h + 1.0e-6);
+      key[a] = d.w[k];
+      pos[a] = a;
+    } else {
+      key[a] = INFINITY;
+      pos[a] = a;
+    }
+  }
+  const double current = inlet_block_sum(cur, part);
+  double applied = volume;
+  if (volume >= 0.0) {
+    // bitonic sort of (stage, position) over INLET_MAX slots
+    for (int size = 2; size <= INLET_MAX; size <<= 1) {
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        __syncthreads();
+        for (int a = t; a < INLET_MAX; a += INLET_TPB) {
+          const int b = a ^ stride;
+          if (b > a) {
+            const bool up = (a & size) == 0;
+            const double ka = key[a], kb = key[b];
+            if ((ka > kb) == up) {
+              key[a] = kb;
+              key[b] = ka;
+              const int pa = pos[a];
+              pos[a] = pos[b];
+              pos[b] = pa;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // cumulative areas of the cells ordered by stage
+    for (int a = t; a < INLET_MAX; a += INLET_TPB) acc[a] = a < n ? d.areas[op.idx[pos[a]]] : 0.0;
+    __syncthreads();
+    inlet_exclusive_scan(acc, part);
+    double sa[INLET_PER];
+#pragma unroll
+    for (int j = 0; j < INLET_PER; j++) {
+      const int a = t * INLET_PER + j;
+      sa[j] = acc[a] + (a < n ? d.areas[op.idx[pos[a]]] : 0.0);     // inclusive
+    }
+    __syncthreads();
+    // volume needed to fill the cells below sorted position a to its stage
+#pragma unroll
+    for (int j = 0; j < INLET_PER; j++) {
+      const int a = t * INLET_PER + j;
+      acc[a] = (a + 1 < n) ? sa[j] * (key[a + 1] - key[a]) : 0.0;
+    }
+    __syncthreads();
+    inlet_exclusive_scan(acc, part);
+    if (t == 0) last = 0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < INLET_PER; j++) {
+      const int a = t * INLET_PER + j;
+      if (a < n && acc[a] <= volume) atomicMax(&last, a);
+    }
+    __syncthreads();
+    const int index = last;
+    // inclusive cumulative area at `index`
+    if (t == index / INLET_PER) part[0] = sa[index % INLET_PER];
+    __syncthreads();
+    const double depth = (volume - acc[index]) / part[0];
+    const double level = key[index] + depth;
+    for (int a = t; a < n; a += INLET_TPB)
+      if (a <= index) d.w[op.idx[pos[a]]] = level;
+  } else if (current + volume >= 0.0) {
+    const double depth = (current + volume) / op.area;
+    for (int a = t; a < n; a += INLET_TPB) {
+      const int k = op.idx[a];
+      d.w[k] = d.z[k] + depth;
+    }
+  } else {
+    for (int a = t; a < n; a += INLET_TPB) {
+      const int k = op.idx[a];
+      d.w[k] = d.z[k];
+      d.uh[k] = 0.0;
+      d.vh[k] = 0.0;
+    }
+    applied = -current;
+  }
+  __syncthreads();
+  if (!(volume < 0.0 && current + volume < 0.0)) {
+#pragma unroll
+    for (int j = 0; j < INLET_PER; j++) {
+      const int a = t + j * INLET_TPB;
+      if (a < n) {
+        const int k = op.idx[a];
+        const double h = d.w[k] - d.z[k];
+        double mx = h * u[j], my = h * v[j];
+        if (op.flags & 1) { mx = h * op.vu; my = h * op.vv; }
+        if (op.flags & 2) { mx = 0.0; my = 0.0; }
+        d.uh[k] = mx;
+        d.vh[k] = my;
+      }
+    }
+  }
+  if (t == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
 }
 
 __global__ void k_clock(Dev d, double t0_unused, cudaGraphConditionalHandle handle, int set_cond) {
@@ -461,9 +644,25 @@ cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_h
   }
   for (size_t i = 0; i < s->ops.size(); i++) {
     const RateOp& op = s->ops[i];
-    LAUNCHK(PH_RATE, k_rate<<<nblk(op.n), TPB, 0, st>>>(d, op.idx, op.n, op.rate, op.factor, (int)i));
+    if (op.kind == 1) {
+      LAUNCHK(PH_RATE, k_inlet<<<1, INLET_TPB, 0, st>>>(d, op, (int)i, op.rate, op.rate, -1.0));
+    } else {
+      LAUNCHK(PH_RATE, k_rate<<<nblk(op.n), TPB, 0, st>>>(d, op.idx, op.n, op.rate, op.factor, (int)i, -1.0));
+    }
   }
   LAUNCH(k_clock<<<1, 1, 0, st>>>(d, 0.0, (cudaGraphConditionalHandle)cond_handle, set_cond ? 1 : 0));
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int i, double rate, double factor, double dt) {
+  const Dev& d = s->d;
+  const RateOp& op = s->ops[i];
+  if (op.n == 0) return cudaSuccess;
+  if (op.kind == 1) {
+    LAUNCHK(PH_RATE, k_inlet<<<1, INLET_TPB, 0, st>>>(d, op, i, rate, factor, dt));
+  } else {
+    LAUNCHK(PH_RATE, k_rate<<<nblk(op.n), TPB, 0, st>>>(d, op.idx, op.n, rate, factor, i, dt));
+  }
   return cudaSuccess;
 }
 

@@ -472,27 +472,32 @@ class Domain:
             self._bind_operators()
 
     def _bind_operators(self):
+        """Register every Rate_operator on the device (indices uploaded once).
+        Constant ones run inside the device step loop; the others are applied
+        from the host step by step (agx_apply_operator) with the rate the
+        host evaluates."""
         self._scn.clear_operators()
         self._dev_ops = []
+        t = self.get_time()
         for op in self.fractional_step_operators:
-            if getattr(op, "device_loop", False) and hasattr(op, "rate"):
-                self._scn.add_rate(op.indices, op.get_rate(), op.get_factor())
-                self._dev_ops.append(op)
+            if hasattr(op, "rate"):
+                self._scn.add_rate(op.indices, op.get_rate(t), op.get_factor(t))
+            elif hasattr(op, "update_Q"):
+                if not hasattr(self._scn, "add_inlet"):
+                    raise NotImplementedError("Inlet_operator runs on the plain FP64 form (precision='fp64')")
+                self._scn.add_inlet(op.indices, op.update_Q(t), op.area, op.flags,
+                                    op.velocity if op.velocity is not None else (0.0, 0.0))
+            else:
+                continue
+            op._dev_index = len(self._dev_ops)
+            self._dev_ops.append(op)
 
-    def _apply_rate_now(self, indices, rate, factor, dt):
-        Q = self.quantities
-        w = Q["stage"].centroid_values
-        sel = slice(None) if indices is None else indices
-        if rate >= 0.0:
-            local = factor * dt * rate
-            w[sel] = w[sel] + local
-        else:
-            heights = w[sel] - Q["elevation"].centroid_values[sel]
-            local = np.maximum(factor * dt * rate, -heights)
-            fac = np.where(local < 0.0, (local + heights) / (heights + 1.0e-10), 1.0)
-            w[sel] = w[sel] + local
-            Q["xmomentum"].centroid_values[sel] *= fac
-            Q["ymomentum"].centroid_values[sel] *= fac
+    def _apply_rate_now(self, op, rate, factor, dt):
+        """One application of a registered Rate_operator on the device."""
+        scn = self._ensure_device()
+        self._push_dirty()
+        scn.apply_operator(op._dev_index, rate, factor, dt)
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c"])
 
     def _device_loop_ok(self):
         if self.boundary_map is None:

@@ -153,6 +153,18 @@ agx_status agx_set_boundary_series(agx_handle h, const double* rows, int64_t n_r
  * rate (operators/rate_operators.py:149-258).  indices == NULL: all cells. */
 agx_status agx_add_rate_operator(agx_handle h, const int32_t* indices, int64_t n, double rate, double factor);
 agx_status agx_clear_operators(agx_handle h);
+/* Inlet_operator (structures/inlet_operator.py:17-165, inlet.py:107-226):
+ * discharge Q (m^3/s) into the cells `indices` (at most 2048) of total area
+ * `area`; flags & 1: momenta from the velocity (velocity_u, velocity_v);
+ * flags & 2: zero velocity.  Applied after each step with the other
+ * operators, in registration order. */
+agx_status agx_add_inlet_operator(agx_handle h, const int32_t* indices, int64_t n, double Q, double area,
+                                  int32_t flags, double velocity_u, double velocity_v);
+/* One application of registered operator `op` (in registration order) with
+ * the values and timestep the caller gives: for a Rate_operator the rate and
+ * factor, for an Inlet_operator Q(t) and Q(t + timestep); used when these are
+ * functions of time evaluated by the host. */
+agx_status agx_apply_operator(agx_handle h, int32_t op, double rate, double factor, double timestep);
 /* Cumulative influx (m^3) of operator `op` (Rate_operator.cumulative_influx). */
 agx_status agx_operator_influx(agx_handle h, int32_t op, double* influx);
 

@@ -12,6 +12,8 @@ The loop mirrors the reference:
 * ``update_timestep``         generic_domain.py:2349-2415
 * ``update_conserved_quantities`` shallow_water/shallow_water_domain.py:2089-2163
 * ``Rate_operator.__call__``  operators/rate_operators.py:149-258 (constant rates)
+* ``Inlet_operator.__call__`` structures/inlet_operator.py:75-165 with
+  structures/inlet.py:107-226 (constant discharge)
 """
 from __future__ import annotations
 
@@ -199,6 +201,8 @@ class OracleDomain:
         self.Dp = ctypes.pointer(D)
         self.boundaries = []
         self.rates = []
+        self.inlets = []
+        self.ops = []              # operators in registration order
         self.relative_time = 0.0
         self.starttime = 0.0
         self.timestep = 0.0
@@ -234,6 +238,61 @@ class OracleDomain:
     def add_rate(self, indices, rate, factor=1.0):
         idx = None if indices is None else np.asarray(indices, np.int64)
         self.rates.append([idx, float(rate), float(factor), 0.0])
+        self.ops.append(("rate", self.rates[-1]))
+
+    def add_inlet(self, indices, Q, velocity=None, zero_velocity=False):
+        """Inlet_operator (structures/inlet_operator.py:17-165): discharge Q
+        (constant, m^3/s) into the cells `indices`."""
+        idx = np.asarray(indices, np.int64)
+        rec = dict(idx=idx, Q=float(Q), velocity=velocity, zero_velocity=bool(zero_velocity),
+                   area=float(np.sum(self.areas[idx])), applied=0.0)
+        self.inlets.append(rec)
+        self.ops.append(("inlet", rec))
+
+    # inlet_operator.py:75-165 with inlet.py:107-226 (set_stages_evenly,
+    # set_depths, get_velocities; velocity_protection = 1e-6, config.py:18)
+    def _apply_inlet(self, r):
+        idx = r["idx"]
+        areas = self.areas[idx]
+        stages = self.stage_c[idx]
+        elev = self.bed_c[idx]
+        depths = stages - elev
+        current_volume = np.sum(depths * areas)
+        total_area = r["area"]
+        Q = 0.5 * (r["Q"] + r["Q"])
+        volume = Q * self.timestep
+        u = self.xmom_c[idx] * depths / (depths * depths + 1.0e-6)
+        v = self.ymom_c[idx] * depths / (depths * depths + 1.0e-6)
+        if volume >= 0.0:
+            order = stages.argsort()
+            summed_areas = np.cumsum(areas[order])
+            summed_volume = np.zeros_like(areas)
+            summed_volume[1:] = np.cumsum(summed_areas[:-1] * np.diff(stages[order]))
+            index = np.nonzero(summed_volume <= volume)[0][-1]
+            depth = (volume - summed_volume[index]) / summed_areas[index]
+            new = stages.copy()
+            new[order[0:index + 1]] = stages[order[index]] + depth
+            self.stage_c[idx] = new
+        elif current_volume + volume >= 0.0:
+            depth = (current_volume + volume) / total_area
+            self.stage_c[idx] = elev + depth
+        else:
+            self.stage_c[idx] = elev
+            self.xmom_c[idx] = 0.0
+            self.ymom_c[idx] = 0.0
+            r["applied"] += -current_volume
+            return
+        d_new = self.stage_c[idx] - elev
+        if r["velocity"] is not None:
+            self.xmom_c[idx] = d_new * r["velocity"][0]
+            self.ymom_c[idx] = d_new * r["velocity"][1]
+        else:
+            self.xmom_c[idx] = d_new * u
+            self.ymom_c[idx] = d_new * v
+        if r["zero_velocity"]:
+            self.xmom_c[idx] = 0.0
+            self.ymom_c[idx] = 0.0
+        r["applied"] += volume
 
     # --- phases ------------------------------------------------------------
     def protect(self):
@@ -313,7 +372,10 @@ class OracleDomain:
         self.timestep = timestep
 
     def apply_fractional_steps(self):
-        for r in self.rates:
+        for kind, r in self.ops:
+            if kind == "inlet":
+                self._apply_inlet(r)
+                continue
             idx, rate, factor = r[0], r[1], r[2]
             if rate >= 0.0:
                 local = factor * self.timestep * rate

@@ -200,7 +200,31 @@ def build_delaunay_rain():
     return d, {"mesh.points": pts, "mesh.elements": tri, "rain.indices": idx, "rain.rate": np.array(0.01)}
 
 
-if __name__ == "__main__":
+def build_inlets(m=12, n=8):
+    # Inlet_operator: inflow over a polygon, extraction with zero velocity,
+    # and a line inlet with an imposed velocity
+    pts, elem, bnd = anuga.rectangular_cross(m, n, 120.0, 80.0)
+    d = anuga.Domain(pts, elem, bnd)
+    d.set_quantity("elevation", lambda x, y: -0.02 * x + 0.1 * np.sin(y / 10.0))
+    d.set_quantity("stage", lambda x, y: np.maximum(-0.02 * x + 0.1 * np.sin(y / 10.0), -1.5))
+    d.set_quantity("friction", 0.02)
+    Br = anuga.Reflective_boundary(d)
+    d.set_boundary({"left": Br, "right": Br, "top": Br, "bottom": Br})
+    a = anuga.Inlet_operator(d, [[10.0, 20.0], [30.0, 20.0], [30.0, 60.0], [10.0, 60.0]], Q=1.5)
+    b = anuga.Inlet_operator(d, [[90.0, 10.0], [110.0, 10.0], [110.0, 30.0], [90.0, 30.0]], Q=-0.4,
+                             zero_velocity=True)
+    c = anuga.Inlet_operator(d, [[50.0, 70.0], [70.0, 70.0]], Q=0.8, velocity=[0.2, 0.0])
+    extra = {"mesh.points": pts, "mesh.elements": elem}
+    for name, op, q in (("a", a, 1.5), ("b", b, -0.4), ("c", c, 0.8)):
+        extra["inlet_%s.indices" % name] = np.asarray(op.inlet.triangle_indices, np.int64)
+        extra["inlet_%s.Q" % name] = np.array(q)
+    d._inlets = (a, b, c)
+    return d, extra
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
+    trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
+elif __name__ == "__main__":
     p, e, b = anuga.rectangular_cross(3, 2, 3.0, 2.0)
     mesh_fixture("mesh_rect_3x2.npz", p, e, b)
     p, e = delaunay_case()
@@ -210,3 +234,4 @@ if __name__ == "__main__":
     trajectory_fixture("traj_dambreak_de0.npz", build_dam_break, "DE0", 1.0, 4.0)
     trajectory_fixture("traj_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 40.0)
     trajectory_fixture("traj_delaunay_rain_de1.npz", build_delaunay_rain, "DE1", 2.0, 6.0)
+    trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)

@@ -84,3 +84,30 @@ def test_oracle_trajectories_bit_exact(golden, oracle_mod, name):
         assert np.array_equal(r[2], f["stage"][i])
         assert np.array_equal(r[3], f["xmom"][i])
         assert np.array_equal(r[4], f["ymom"][i])
+
+
+INLETS = {"a": dict(), "b": dict(zero_velocity=True), "c": dict(velocity=(0.2, 0.0))}
+
+
+def test_oracle_inlets_bit_exact(golden, oracle_mod):
+    """Inlet_operator (inflow over a polygon, extraction with zero velocity, a
+    line inlet with an imposed velocity) against the reference's trajectory."""
+    f = golden("traj_inlets_de1.npz")
+    p, e = f["mesh.points"], f["mesh.elements"]
+    p2, e2, b = rectangular_cross(12, 8, 120.0, 80.0)
+    assert np.array_equal(p, p2) and np.array_equal(e, e2)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, "DE1")
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    od.set_boundaries([(M.tag_boundary_cells[t], "reflective", None) for t in M.tag_boundary_cells])
+    for k, kw in INLETS.items():
+        od.add_inlet(f["inlet_%s.indices" % k], float(f["inlet_%s.Q" % k]), **kw)
+    res = [(t, od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy(), od.ymom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["times"])
+    assert [r[1] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[2], f["stage"][i]), i
+        assert np.array_equal(r[3], f["xmom"][i]), i
+        assert np.array_equal(r[4], f["ymom"][i]), i
