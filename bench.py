@@ -382,9 +382,9 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # category's launches of one step, divided by the cells of the captured mesh).
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
-        "bytes_per_cell": (117.2096e6 + 10.04544e6 + 177.274112e6 + 24.079616e6) / 1.0e6,
+        "bytes_per_cell": (117.267712e6 + 11.5648e6 + 177.335808e6 + 25.904384e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
-                "(m=500, MINB=3 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
+                "(m=500, MINB=4 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
                 "scaled by cells; profiles/k_pool_flux_inflow_bumps_1M_mixed.md"},
 }
 
