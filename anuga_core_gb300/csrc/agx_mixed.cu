@@ -796,6 +796,7 @@ struct ScnHost {
   int N = 0, B = 0, tile0 = 0, ntile = 0, bnd0 = 0, halo0 = 0, nhalo = 0;
   agx_params prm{};
   int* order = nullptr;          // device [N]: original index of each stored cell
+  int* inv = nullptr;            // device [N]: stored index of each original cell
   double* series = nullptr;
   std::vector<PoolOp> ops;
   bool work_dirty = true;
@@ -1082,6 +1083,7 @@ agx_status agx_pool_destroy(agx_pool p) {
   if (p->graph) cudaGraphDestroy(p->graph);
   for (auto& s : p->scn) {
     if (s.order) cudaFree(s.order);
+    if (s.inv) cudaFree(s.inv);
     if (s.series) cudaFree(s.series);
     for (auto& op : s.ops) if (op.idx) cudaFree((void*)op.idx);
   }
@@ -1202,6 +1204,16 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
   sh = ScnHost();
   PCK(cudaMalloc(&sh.order, N * 4));
   PCK(cudaMemcpyAsync(sh.order, order, N * 4, cudaMemcpyHostToDevice, st));
+  {
+    std::vector<int32_t> iv((size_t)N, -1);
+    for (int64_t j = 0; j < N; j++) {
+      if (order[j] < 0 || order[j] >= N || iv[order[j]] >= 0) return pfail(AGX_E_INVALID, "order is not a permutation");
+      iv[order[j]] = (int32_t)j;
+    }
+    PCK(cudaMalloc(&sh.inv, N * 4));
+    PCK(cudaMemcpyAsync(sh.inv, iv.data(), N * 4, cudaMemcpyHostToDevice, st));
+    PCK(cudaStreamSynchronize(st));
+  }
   if (B > 0) {
     std::vector<int32_t> bc(B);
     for (int64_t m = 0; m < B; m++) bc[m] = bcell[m] + c0;
@@ -1269,6 +1281,7 @@ agx_status agx_pool_remove(agx_pool p, int32_t sid) {
   p->scn_host[sid].active = 0;
   if ((st = push_scn(p))) return st;
   if (sh.order) cudaFree(sh.order);
+  if (sh.inv) cudaFree(sh.inv);
   if (sh.series) cudaFree(sh.series);
   bool had_ops = !sh.ops.empty();
   for (auto& op : sh.ops) if (op.idx) cudaFree((void*)op.idx);
@@ -1342,9 +1355,46 @@ __global__ void k_scatter3(double* dst, const double* w, const double* uh, const
   }
 }
 
+// Page-locked host memory the device can address at the same virtual
+// address (cudaPointerGetAttributes: host memory with a device pointer equal
+// to the host pointer).  Kernels then read or write it directly over the
+// host link; other (pageable) buffers go through copies.
+static bool host_mapped(const void* ptr) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer == ptr;
+}
+
+// Direct exchange with mapped host buffers, walked in the caller's order
+// (contiguous on the host side; permuted on the device side).
+__global__ void k_state_from_host(double* w, double* uh, double* vh, const double* hw, const double* huh,
+                                  const double* hvh, const int* inv, int n) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < n) {
+    const int j = inv[o];
+    w[j] = hw[o];
+    uh[j] = huh[o];
+    vh[j] = hvh[o];
+  }
+}
+__global__ void k_state_to_host(double* hw, double* huh, double* hvh, const double* w, const double* uh,
+                                const double* vh, const int* inv, int n) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < n) {
+    const int j = inv[o];
+    hw[o] = w[j];
+    huh[o] = uh[j];
+    hvh[o] = vh[j];
+  }
+}
+
 // The conserved state (stage, xmomentum, ymomentum) in the caller's cell
-// order, in one call: three copies through the staging buffer, one
-// permutation kernel, one synchronisation.
+// order, in one call with one synchronisation: read by one kernel straight
+// from page-locked host buffers, or else three copies through the staging
+// buffer and one permutation kernel.
 agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const double* uh, const double* vh, int64_t n) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !w || !uh || !vh)
     return pfail(AGX_E_INVALID, "bad arguments");
@@ -1352,6 +1402,14 @@ agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const do
   if (n != sh.N) return pfail(AGX_E_INVALID, "the state has %d cells", sh.N);
   const int c0 = sh.tile0 * TILE;
   cudaStream_t st = p->stream;
+  if (host_mapped(w) && host_mapped(uh) && host_mapped(vh)) {
+    k_state_from_host<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, w, uh, vh,
+                                                    sh.inv, (int)n);
+    count_launch();
+    PCK(cudaGetLastError());
+    sh.work_dirty = true;
+    return psync(p);
+  }
   PCK(cudaMemcpyAsync(p->staging, w, n * 8, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync(p->staging + n, uh, n * 8, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync(p->staging + 2 * n, vh, n * 8, cudaMemcpyHostToDevice, st));
@@ -1369,6 +1427,13 @@ agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, do
   if (n != sh.N) return pfail(AGX_E_INVALID, "the state has %d cells", sh.N);
   const int c0 = sh.tile0 * TILE;
   cudaStream_t st = p->stream;
+  if (host_mapped(w) && host_mapped(uh) && host_mapped(vh)) {
+    k_state_to_host<<<nblk1((int)n), 256, 0, st>>>(w, uh, vh, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, sh.inv,
+                                                  (int)n);
+    count_launch();
+    PCK(cudaGetLastError());
+    return psync(p);
+  }
   k_scatter3<<<nblk1((int)n), 256, 0, st>>>(p->staging, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, sh.order, (int)n);
   count_launch();
   PCK(cudaGetLastError());

@@ -371,7 +371,10 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
     e2e_value = world * N * args.steps / (e2e_ms / 1e3)
     out = {"precision": precision, "cells": N, "value": value, "ms_per_step": ms_per_step, "roofline": roof,
            "step_roofline": step_roof, "launches": launches, "autotune": tune, "state_bytes": scn_bytes(d),
-           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N}}
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
+                   "path": "conserved state w, uh, vh from and to page-locked host buffers each step through "
+                           "agx_set_state/agx_get_state (the mixed pool reads and writes mapped host memory "
+                           "directly; the plain path copies)"}}
     del d, scn
     torch.cuda.synchronize()
     return out

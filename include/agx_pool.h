@@ -55,7 +55,9 @@ agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t field, const doub
 agx_status agx_pool_get_field(agx_pool p, int32_t sid, int32_t field, double* host, int64_t n);
 
 /* The conserved state (stage, xmomentum, ymomentum; N values each) in one
- * call with one synchronisation. */
+ * call with one synchronisation.  Page-locked host buffers the device maps at
+ * the same address are read or written by one kernel directly; other buffers
+ * go through copies. */
 agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const double* uh, const double* vh, int64_t n);
 agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, double* vh, int64_t n);
 

@@ -193,3 +193,26 @@ def test_state_exchange_in_one_call_matches_per_field():
     scn.set_state(w2, uh2, vh2)
     for name, ref in (("stage_c", w2), ("xmom_c", uh2), ("ymom_c", vh2)):
         assert np.array_equal(scn.get(name), ref), name
+
+
+def test_state_exchange_with_page_locked_buffers():
+    """Page-locked host buffers are read and written by the device directly;
+    the values are the same as through the copying path."""
+    import torch
+    d = workloads.dam_break(m=30, flow_algorithm="DE1", precision="mixed")
+    for _ in d.evolve(yieldstep=0.5, finaltime=0.5):
+        pass
+    scn = d._scn
+    N = len(d)
+    pin = [torch.empty(N, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    scn.get_state(*pin)
+    ref = scn.get_state()                      # pageable numpy arrays: the copying path
+    for a, b in zip(pin, ref):
+        assert np.array_equal(a, b)
+    rng = np.random.default_rng(4)
+    new = [ref[0] + 0.01 * rng.uniform(size=N), ref[1] * 0.5, ref[2] * 0.25]
+    for a, b in zip(pin, new):
+        a[:] = b
+    scn.set_state(*pin)
+    for name, b in zip(("stage_c", "xmom_c", "ymom_c"), new):
+        assert np.array_equal(scn.get(name), b), name
