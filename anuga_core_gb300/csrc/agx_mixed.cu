@@ -31,7 +31,7 @@
 
 namespace agx {
 
-constexpr int TILE = 256;
+constexpr int TILE = 128;
 
 struct PoolScn {             // device-resident per-scenario record
   Clock clock;
@@ -44,7 +44,7 @@ struct PoolScn {             // device-resident per-scenario record
   int pad[3];
 };
 
-constexpr int HALO_MAX = 256;   // halo cells a tile stages in shared memory
+constexpr int HALO_MAX = 128;   // halo cells a tile stages in shared memory
 constexpr int LNK_INLINE = 1023;
 
 struct PoolDev {
@@ -949,8 +949,8 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->variant == 0) k_pool_flux<false, 3><<<Gf, TILE, 0, st>>>(d);
-  else k_pool_flux<false, 4><<<Gf, TILE, 0, st>>>(d);
+  if (p->variant == 0) k_pool_flux<false, 6><<<Gf, TILE, 0, st>>>(d);
+  else k_pool_flux<false, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
   k_pool_timestep<<<nblk1(S), 256, 0, st>>>(d, S);
@@ -962,8 +962,8 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   k_pool_update<<<std::max(d.ntiles, 1), TILE, 0, st>>>(d, 0);
   count_launch();
   phase_mark(st, PH_UPDATE);
-  if (p->variant == 0) k_pool_flux<true, 3><<<Gf, TILE, 0, st>>>(d);
-  else k_pool_flux<true, 4><<<Gf, TILE, 0, st>>>(d);
+  if (p->variant == 0) k_pool_flux<true, 6><<<Gf, TILE, 0, st>>>(d);
+  else k_pool_flux<true, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
   for (size_t s = 0; s < p->scn.size(); s++) {
@@ -1052,8 +1052,8 @@ agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
   if (st) return st;
   int sms = 0, per = 0, per4 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false, 3>, TILE, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pool_flux<false, 4>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false, 6>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pool_flux<false, 8>, TILE, 0);
   p->grid = std::max(1, sms * std::max(per, 1));
   p->grid_v[0] = p->grid;
   p->grid_v[1] = std::max(1, sms * std::max(per4, 1));

@@ -246,8 +246,8 @@ def pack_mixed_numpy(mesh, order=None):
                 boundary_cell=np.ascontiguousarray(bcell.astype(np.int32)))
 
 
-TILE = 256
-HALO_MAX = 256          # halo cells a tile can stage in shared memory
+TILE = 128
+HALO_MAX = 128          # halo cells a tile can stage in shared memory
 LNK_INLINE = 1023       # local index meaning "reconstruct this neighbour inline"
 
 

@@ -37,7 +37,7 @@ agx_status agx_pool_set_stream(agx_pool p, void* stream);
 
 /* Add a scenario (Domain construction, shallow_water_domain.py:231):
  * conn[N*4], geo[N*16], area[N], order[N], boundary_cell[B], lnk[N],
- * halo_off/halo_cnt per tile of 256 cells, halo_cells[n_halo]. */
+ * halo_off/halo_cnt per tile of 128 cells, halo_cells[n_halo]. */
 agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, const float* geo,
                         const double* area, const int32_t* order, const int32_t* boundary_cell,
                         const int32_t* lnk, const int32_t* halo_off, const int32_t* halo_cnt, int64_t n_halo,
