@@ -426,6 +426,10 @@ def run_batch(args, torch, rank, world, local, dist):
     value = N * args.steps / (ms / 1e3)
     hbm, peak_kind = _peaks()
     ach = ALG_BYTES_PER_CELL_STEP["mixed"] * N / (ms / args.steps / 1e3) / 1e9
+    dominant = max(phases, key=phases.get)
+    kb = KERNEL_BYTES_PER_CELL["mixed"].get(dominant)
+    ach_k = kb * N / (phases[dominant] / 1e3) / 1e9 if kb else None
+    tr = TRAFFIC_PER_STEP.get(("mixed", dominant))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
@@ -433,8 +437,14 @@ def run_batch(args, torch, rank, world, local, dist):
                        "DE1 mixed, one pool" % (len(doms), N), "cells": N, "scenarios": len(doms),
                        "setup_s": setup_s, "draw": info["draw"], "l2": "inputs larger than L2",
                        "autotune": {"chosen": best, "s_per_step": res}},
-            "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "peak_kind": peak_kind, "traffic": None, "phase_ms": phases},
+            "roofline": {"bound": "hbm", "achieved": ach_k, "peak": hbm, "unit": "GB/s",
+                         "frac": ach_k / hbm if ach_k else None, "peak_kind": peak_kind,
+                         "traffic": tr["bytes_per_cell"] * N if tr else None,
+                         "traffic_note": tr["note"] if tr else None,
+                         "kernel": "%s (%.1f%% of step time)" % (dominant, 100.0 * phases[dominant] / max(sum(phases.values()), 1e-9)),
+                         "kernel_ms_per_step": phases[dominant], "alg_bytes_per_cell": kb, "phase_ms": phases},
+            "step_roofline": {"achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                              "note": "352 algorithmic B/cell-step of the ideal fused step x cells / step time"},
             "gpu_launches": int(launches), "clocks": clocks}
     print(json.dumps(line))
 
