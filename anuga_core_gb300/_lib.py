@@ -91,6 +91,9 @@ def load(path=None):
         "agx_get_field": ([H, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_device_ptr": ([H, ctypes.c_int32, P(ctypes.c_void_p), P(ctypes.c_int64)], ctypes.c_int32),
         "agx_set_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
+        "agx_sww_bind": ([H, ctypes.c_int64, _i32p, _i32p], ctypes.c_int32),
+        "agx_sww_frame": ([H, ctypes.c_double, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+                          ctypes.c_int32),
         "agx_get_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary": ([H, _i32p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary_series": ([H, _f64p, ctypes.c_int64], ctypes.c_int32),
@@ -230,6 +233,20 @@ class Scenario:
         out = [np.empty(self.N) if x is None else x for x in (w, uh, vh)]
         check(self.L.agx_get_state(self.h, ptr_f64(out[0]), ptr_f64(out[1]), ptr_f64(out[2]), self.N))
         return out
+
+    def sww_bind(self, node_offsets, node_slots):
+        off = np.ascontiguousarray(node_offsets, np.int32)
+        sl = np.ascontiguousarray(node_slots, np.int32)
+        check(self.L.agx_sww_bind(self.h, off.size - 1, ptr_i32(off), ptr_i32(sl)))
+        self._sww_P = off.size - 1
+
+    def sww_frame(self, min_storable_height):
+        """(vertex [3, P], centroid [3, N]) float32 output frame."""
+        fp = ctypes.POINTER(ctypes.c_float)
+        v = np.empty((3, self._sww_P), np.float32)
+        c = np.empty((3, self.N), np.float32)
+        check(self.L.agx_sww_frame(self.h, float(min_storable_height), v.ctypes.data_as(fp), c.ctypes.data_as(fp)))
+        return v, c
 
     def device_ptr(self, name):
         p = ctypes.c_void_p()

@@ -322,6 +322,9 @@ agx_status agx_scenario_destroy(agx_handle h) {
   destroy_graph(s);
   for (auto& op : s->ops)
     if (op.idx) cudaFree(op.idx);
+  if (s->node_off) cudaFree(s->node_off);
+  if (s->node_slot) cudaFree(s->node_slot);
+  if (s->frame) cudaFree(s->frame);
   if (s->bseries) cudaFree(s->bseries);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream) cudaStreamSynchronize(s->own_stream);
@@ -367,6 +370,39 @@ agx_status agx_get_state(agx_handle h, double* w, double* uh, double* vh, int64_
   CK(cudaMemcpyAsync(w, h->field[AGX_STAGE_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(uh, h->field[AGX_XMOM_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(vh, h->field[AGX_YMOM_C], (size_t)n * 8, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h);
+}
+
+agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, const int32_t* node_slots) {
+  if (!h || P < 0 || (P > 0 && (!node_offsets || !node_slots))) return fail(AGX_E_INVALID, "bad arguments");
+  if (node_offsets[0] != 0 || node_offsets[P] != 3 * (int64_t)h->N)
+    return fail(AGX_E_INVALID, "node offsets must run from 0 to 3N");
+  for (int64_t p = 0; p < P; p++)
+    if (node_offsets[p + 1] < node_offsets[p]) return fail(AGX_E_INVALID, "node offsets must not decrease");
+  for (int64_t q = 0; q < 3 * (int64_t)h->N; q++)
+    if (node_slots[q] < 0 || node_slots[q] >= 3 * h->N) return fail(AGX_E_INVALID, "vertex slot out of range");
+  agx_status st = sync(h);
+  if (st) return st;
+  if (h->node_off) cudaFree(h->node_off);
+  if (h->node_slot) cudaFree(h->node_slot);
+  if (h->frame) cudaFree(h->frame);
+  h->node_off = h->node_slot = nullptr;
+  h->frame = nullptr;
+  h->P = (int)P;
+  CK(cudaMalloc(&h->node_off, (size_t)(P + 1) * 4));
+  CK(cudaMalloc(&h->node_slot, (size_t)3 * h->N * 4 + 4));
+  CK(cudaMalloc(&h->frame, ((size_t)3 * P + 3 * (size_t)h->N) * 4 + 4));
+  CK(cudaMemcpyAsync(h->node_off, node_offsets, (size_t)(P + 1) * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->node_slot, node_slots, (size_t)3 * h->N * 4, cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out) {
+  if (!h || !vertex_out || !centroid_out) return fail(AGX_E_INVALID, "bad arguments");
+  if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
+  CK(enqueue_sww_frame(h, h->stream, min_storable_height));
+  if (h->P > 0) CK(cudaMemcpyAsync(vertex_out, h->frame, (size_t)3 * h->P * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(centroid_out, h->frame + 3 * (size_t)h->P, (size_t)3 * h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   return sync(h);
 }
 

@@ -148,6 +148,11 @@ struct Dev {
 struct Scenario {
   int device = 0;
   int N = 0, B = 0, E = 0;
+  // sww output: node -> vertex-slot CSR and a float staging buffer
+  int P = 0;
+  int* node_off = nullptr;
+  int* node_slot = nullptr;
+  float* frame = nullptr;
   agx_params prm{};
   Dev d{};
   void* arena = nullptr;
@@ -185,6 +190,7 @@ cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_h
 cudaError_t enqueue_distribute(Scenario* s, cudaStream_t st, bool with_protect, bool vertices);
 cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
 cudaError_t enqueue_op(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
+cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double min_storable_height);
 cudaError_t enqueue_protect(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_boundary(Scenario* s, cudaStream_t st, double t_override, bool stage2);
 cudaError_t enqueue_fluxes(Scenario* s, cudaStream_t st, int substep);

@@ -524,6 +524,38 @@ __global__ void __launch_bounds__(INLET_TPB) k_inlet(Dev d, RateOp op, int slot,
   if (t == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
 }
 
+// One sww frame (file/sww.py:352-368 store_timestep with smoothed vertex
+// values): per node the mean of its vertex slots, summed in slot order (as
+// numpy.bincount does), stage masked to the bed where the depth is below
+// minimum_storable_height; centroid values masked the same way; all as float.
+__global__ void k_sww_nodes(Dev d, int P, const int* off, const int* slot, double msh, float* out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  double aw = 0.0, au = 0.0, av = 0.0;
+  const int a = off[p], b = off[p + 1];
+  for (int q = a; q < b; q++) {
+    const int s = slot[q];
+    const double w = d.wv[s], z = d.zv[s];
+    aw += (w - z < msh) ? z : w;
+    au += d.uhv[s];
+    av += d.vhv[s];
+  }
+  const double c = b > a ? (double)(b - a) : 1.0;
+  out[p] = (float)(aw / c);
+  out[P + p] = (float)(au / c);
+  out[2 * P + p] = (float)(av / c);
+}
+
+__global__ void k_sww_cells(Dev d, double msh, float* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  const double w = d.w[k], z = d.z[k];
+  out[k] = (float)((w - z < msh) ? z : w);
+  out[d.N + k] = (float)d.uh[k];
+  out[2 * d.N + k] = (float)d.vh[k];
+}
+
+
 __global__ void k_clock(Dev d, double t0_unused, cudaGraphConditionalHandle handle, int set_cond) {
   (void)t0_unused;
   const int reason = clock_logic(d.clock);
@@ -663,6 +695,13 @@ cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int i, double rate, 
   } else {
     LAUNCHK(PH_RATE, k_rate<<<nblk(op.n), TPB, 0, st>>>(d, op.idx, op.n, rate, factor, i, dt));
   }
+  return cudaSuccess;
+}
+
+cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double msh) {
+  const Dev& d = s->d;
+  if (s->P > 0) LAUNCH(k_sww_nodes<<<nblk(s->P), TPB, 0, st>>>(d, s->P, s->node_off, s->node_slot, msh, s->frame));
+  if (d.N > 0) LAUNCH(k_sww_cells<<<nblk(d.N), TPB, 0, st>>>(d, msh, s->frame + 3 * (size_t)s->P));
   return cudaSuccess;
 }
 

@@ -9,9 +9,12 @@ elevation, friction, stage, xmomentum, ymomentum in single precision, the
 values are stored smoothed (averaged per node), the reference's default
 (``set_store_vertices_uniquely(False)``).
 
-The state is read from the device at each yield (one D2H copy per stored
-array).  NetCDF classic format is written with scipy.io.netcdf_file (the
-netCDF4 package is not required).
+On the plain FP64 form the frame is formed on the device (agx_sww_frame:
+storable-height mask, node means summed in the same order as numpy's
+bincount, single precision) and read back with one copy of 3 floats per node
+and 3 per cell; the mixed form builds it on the host from the quantities'
+vertex values.  NetCDF classic format is written with scipy.io.netcdf_file
+(the netCDF4 package is not required).
 """
 from __future__ import annotations
 
@@ -38,6 +41,22 @@ class SWW_file:
         self._count = np.bincount(tri.ravel(), minlength=self.P).astype(float)
         self._count[self._count == 0] = 1.0
 
+    def _device_frame(self):
+        """(vertex [3, P], centroid [3, N]) float32 from the device, or None."""
+        d = self.domain
+        scn = d._scn
+        if scn is None or not hasattr(scn, "sww_frame"):
+            return None
+        if not getattr(self, "_bound", False):
+            slots = np.argsort(self._tri.ravel(), kind="stable")
+            counts = np.bincount(self._tri.ravel(), minlength=self.P)
+            off = np.zeros(self.P + 1, np.int64)
+            off[1:] = np.cumsum(counts)
+            scn.sww_bind(off, slots)
+            self._bound = True
+        d._push_dirty()
+        return scn.sww_frame(d.minimum_storable_height)
+
     def _smooth(self, vertex_values):
         acc = np.bincount(self._tri.ravel(), weights=vertex_values.ravel(), minlength=self.P)
         return acc / self._count
@@ -48,11 +67,11 @@ class SWW_file:
         f.institution = "anuga_core_gb300"
         f.description = "Output from anuga_core_gb300 (DE timestep on GPU)"
         f.starttime = d.starttime
+        f.createDimension("number_of_timesteps", None)      # the record dimension comes first
         f.createDimension("number_of_volumes", self.N)
         f.createDimension("number_of_vertices", 3)
         f.createDimension("number_of_points", self.P)
         f.createDimension("numbers_in_range", 2)
-        f.createDimension("number_of_timesteps", None)
         x = f.createVariable("x", "f", ("number_of_points",))
         y = f.createVariable("y", "f", ("number_of_points",))
         x[:] = d.mesh.nodes[:, 0].astype(np.float32)
@@ -83,25 +102,49 @@ class SWW_file:
         t = f.variables["time"]
         i = t.shape[0]
         t[i] = d.get_time() - d.starttime
+        frame = self._device_frame()
         Q = d.quantities
-        zv = Q["elevation"].vertex_values
-        for q in DYNAMIC:
-            vv = Q[q].vertex_values
-            if q == "stage":
-                # minimum_storable_height mask (file/sww.py:352-368)
-                vv = np.where(vv - zv < d.minimum_storable_height, zv, vv)
-            A = self._smooth(vv).astype(np.float32)
+        zv = Q["elevation"].vertex_values if frame is None else None
+        for j, q in enumerate(DYNAMIC):
+            if frame is not None:
+                A = frame[0][j]
+            else:
+                vv = Q[q].vertex_values
+                if q == "stage":
+                    # minimum_storable_height mask (file/sww.py:352-368)
+                    vv = np.where(vv - zv < d.minimum_storable_height, zv, vv)
+                A = self._smooth(vv).astype(np.float32)
             f.variables[q][i, :] = A
             r = f.variables[q + "_range"]
             r[0] = min(float(r[0]), float(A.min()) if A.size else np.inf)
             r[1] = max(float(r[1]), float(A.max()) if A.size else -np.inf)
             if self.store_centroids:
-                c = Q[q].centroid_values
-                if q == "stage":
-                    zc = Q["elevation"].centroid_values
-                    c = np.where(c - zc < d.minimum_storable_height, zc, c)
-                f.variables[q + "_c"][i, :] = c.astype(np.float32)
+                if frame is not None:
+                    c = frame[1][j]
+                else:
+                    c = Q[q].centroid_values
+                    if q == "stage":
+                        zc = Q["elevation"].centroid_values
+                        c = np.where(c - zc < d.minimum_storable_height, zc, c)
+                f.variables[q + "_c"][i, :] = np.asarray(c, np.float32)
         f.close()
+
+    def host_frame(self):
+        """The same frame formed on the host from the quantities (reference)."""
+        d = self.domain
+        Q = d.quantities
+        zv = Q["elevation"].vertex_values
+        zc = Q["elevation"].centroid_values
+        V, C = [], []
+        for q in DYNAMIC:
+            vv = Q[q].vertex_values
+            c = Q[q].centroid_values
+            if q == "stage":
+                vv = np.where(vv - zv < d.minimum_storable_height, zv, vv)
+                c = np.where(c - zc < d.minimum_storable_height, zc, c)
+            V.append(self._smooth(vv).astype(np.float32))
+            C.append(c.astype(np.float32))
+        return np.array(V), np.array(C)
 
 
 def read_sww(filename):

@@ -220,6 +220,17 @@ agx_status agx_time_phases(agx_handle h, int32_t reps, double* ms, int32_t n_cat
 /* Read the statistics without stepping. */
 agx_status agx_get_stats(agx_handle h, agx_step_stats* out);
 
+/* ---- sww output (file/sww.py:260-435 store_timestep, smoothed vertices) ------- */
+/* Node -> vertex-slot map: the vertex slots 3k+i of node p are
+ * node_slots[node_offsets[p] .. node_offsets[p+1]) in increasing order. */
+agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, const int32_t* node_slots);
+/* One output frame from the device state (vertex values as last
+ * distributed): vertex_out[3P] = stage, xmomentum, ymomentum per node (mean
+ * of its vertex slots, stage set to the bed where the depth is below
+ * min_storable_height), centroid_out[3N] the same quantities per cell;
+ * single precision, one device-to-host copy each. */
+agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 int32_t agx_last_error(char* buf, int32_t n);
 int32_t agx_version(void);
