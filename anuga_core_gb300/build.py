@@ -27,7 +27,6 @@ UNITS = [
     ("agx_plain.cu", ["--fmad=false"]),
     ("agx_api.cu", ["--fmad=false"]),
     ("agx_mixed.cu", ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"]),
-    ("agx_batch.cu", []),
     ("agx_noalloc.cu", ["--fmad=false"]),
     ("agx_probe.cu", []),
 ]

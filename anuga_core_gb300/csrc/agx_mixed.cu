@@ -944,7 +944,6 @@ static int nblk1(int n) { return (n + 255) / 256; }
 
 static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
   const PoolDev& d = p->d;
-  const int G = p->grid;
   const int S = p->cap_scn;
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
