@@ -365,25 +365,29 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   __shared__ double shd[TILE / 32];
   const float4* W = FUSED2 ? d.W1 : d.W0;
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int base = tile * TILE;
+    const int k = base + threadIdx.x;
+    // the own cell's tables are loaded before the tile's scenario is known
+    const int4 cn_s = d.conn[k];
+    const int lk_s = d.lnk[k];
+    const float4 rk_s = W[k];
+    const int2 ht = d.tile_halo[tile];
     const int sid = d.tile_scn[tile];
     if (sid < 0) continue;
     PoolScn* S = d.scn + sid;
     if (!S->active) continue;
     if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
     const MParams P = S->P;
-    const int base = tile * TILE;
-    const int k = base + threadIdx.x;
     const bool valid = k < S->cell0 + S->ncell;
     bool sdry = false;
     float4 rk = make_float4(0.f, 0.f, 0.f, 0.f);
     EdgeState own[3];
-    const int2 ht = d.tile_halo[tile];
     int4 cn = make_int4(-1, -1, -1, 0);
     int lk = 0;
     if (valid) {
-      cn = d.conn[k];
-      lk = d.lnk[k];
-      rk = W[k];
+      cn = cn_s;
+      lk = lk_s;
+      rk = rk_s;
       const bool b0 = cn.x < 0, b1 = cn.y < 0, b2 = cn.z < 0;
       const float4 r0 = b0 ? rk : W[cn.x];
       const float4 r1 = b1 ? rk : W[cn.y];
@@ -564,22 +568,26 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
 __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
   (void)unused;
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+    const int k = tile * TILE + threadIdx.x;
+    // the cell's data are loaded before the tile's scenario is known (every
+    // index of a used tile lies inside the pool's arrays)
+    double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
+    const double z = d.z[k];
+    const float etak = d.eta[k];
+    const float4 Ek = d.E[k];
     const int sid = d.tile_scn[tile];
     if (sid < 0) continue;
     PoolScn* S = d.scn + sid;
     if (!S->active) continue;
     const MParams P = S->P;
     const int euler = !P.rk2;
-    const int k = tile * TILE + threadIdx.x;
     const bool valid = k < S->cell0 + S->ncell;
     int neg = 0;
     double added = 0.0;
     if (valid) {
       const double dt = S->clock.timestep;
-      double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
-      const double z = d.z[k];
       double depth1;
-      neg = update_lean(P, w, uh, vh, z, d.area + k, d.eta[k], d.E[k], dt, (float)dt, added, depth1);
+      neg = update_lean(P, w, uh, vh, z, d.area + k, etak, Ek, dt, (float)dt, added, depth1);
       const float4 r = record_of(P, depth1, uh, vh);
       if (euler) {
         d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh;
