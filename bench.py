@@ -40,6 +40,23 @@ UNIT = "cell-steps/s"
 ALG_BYTES_PER_CELL_STEP = {"fp64": 488.0, "mixed": 352.0}
 
 
+def max_over_ranks(ms, dist):
+    """The slowest rank's time: each rank is an independent replica (no
+    data-path collective); the job's time is the maximum over ranks."""
+    if dist is None:
+        return ms
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells_per_rank, steps, ms_max, world):
+    """Whole-job throughput: every rank advances its own replica."""
+    return world * cells_per_rank * steps / (ms_max / 1e3)
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -314,12 +331,9 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
     barrier()
     ms = e0.elapsed_time(e1)
     launches = _lib.kernel_launches() - launches0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     ms_per_step = ms / args.steps
-    value = world * N * args.steps / (ms / 1e3)
+    value = replica_value(N, args.steps, ms, world)
 
     # per-kernel CUDA-event timing (direct launches on the same stream)
     phases = scn.time_phases(reps=3)
@@ -367,8 +381,8 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
         scn.get_state(w, uh, vh)
     e3.record(stream)
     barrier()
-    e2e_ms = e2.elapsed_time(e3)
-    e2e_value = world * N * args.steps / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(e2.elapsed_time(e3), dist)
+    e2e_value = replica_value(N, args.steps, e2e_ms, world)
     out = {"precision": precision, "cells": N, "value": value, "ms_per_step": ms_per_step, "roofline": roof,
            "step_roofline": step_roof, "launches": launches, "autotune": tune, "state_bytes": scn_bytes(d),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
@@ -420,10 +434,10 @@ def run_batch(args, torch, rank, world, local, dist):
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist)
     launches = _lib.kernel_launches() - launches0
     phases = B.pool.time_phases(reps=2)
-    value = N * args.steps / (ms / 1e3)
+    value = replica_value(N, args.steps, ms, world)
     hbm, peak_kind = _peaks()
     ach = ALG_BYTES_PER_CELL_STEP["mixed"] * N / (ms / args.steps / 1e3) / 1e9
     dominant = max(phases, key=phases.get)
@@ -446,7 +460,10 @@ def run_batch(args, torch, rank, world, local, dist):
             "step_roofline": {"achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                               "note": "352 algorithmic B/cell-step of the ideal fused step x cells / step time"},
             "gpu_launches": int(launches), "clocks": clocks}
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def run_serve(args, torch):
