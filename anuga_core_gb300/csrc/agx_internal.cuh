@@ -16,6 +16,7 @@ constexpr int MAX_OPS = 16;
 struct Clock {
   double time, yield_time, final_time;   // final_time < 0: none
   double timestep, flux_timestep;
+  float timestep32, pad_ts;              // (float)timestep, for the mixed-precision kernels
   double recorded_min, recorded_max;
   double cfl, max_dt, min_dt;
   double mass_added;
@@ -66,6 +67,7 @@ __host__ __device__ inline void timestep_logic(Clock* c) {
   if (c->final_time >= 0.0 && c->time + ts > c->final_time) ts = c->final_time - c->time;
   if (c->time + ts > c->yield_time) ts = c->yield_time - c->time;
   c->timestep = ts;
+  c->timestep32 = (float)ts;
 }
 
 // End of one step (generic_domain.py:1851-1912): advance time, count, and

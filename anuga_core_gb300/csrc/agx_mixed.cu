@@ -234,12 +234,12 @@ __device__ void series_at(const double* rows, int n, double t, double out[3]) {
 // Manning friction as the factor x with q_new = q_tmp * (1 - x):
 // q_new = q_tmp / (1 - dt S), S = -g eta^2 |q| / h^(7/3)  (sw_domain_openmp.c:1954-1986,
 // quantity.c:772-818).  x = a / (1 + a), a = -dt S >= 0.
-__device__ __forceinline__ float manning_x(const MParams& P, float h, float uh, float vh, float eta, double dt) {
+__device__ __forceinline__ float manning_x(const MParams& P, float h, float uh, float vh, float eta, float dt32) {
   if (!(eta > P.hmin) || !(h >= P.hmin)) return 0.0f;
   const float mom = sqrtf(uh * uh + vh * vh);
   const float h73 = h * h * cbrtf(h);
   const float S = P.g * eta * eta * mom / h73;     // -S
-  const float a = (float)dt * S;
+  const float a = dt32 * S;
   if (!(a < 1.0e30f)) return 1.0f;
   return a / (1.0f + a);
 }
@@ -271,6 +271,21 @@ __device__ __forceinline__ float d2f_bits(double x) {
 }
 
 __device__ __forceinline__ bool negative_bits(double x) { return __double_as_longlong(x) < 0; }
+
+// 0.5 a + 0.5 b with one FP64 add: halving by decrementing the exponent is
+// exact for normal numbers, so the result is bitwise that of the product form
+// (which rounds once, after two exact halvings); zero, subnormal and
+// non-finite operands take the product form.
+__device__ __forceinline__ double half_sum(double a, double b) {
+  const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+  const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);
+  const double s = a + b;
+  const long long bits = __double_as_longlong(s);
+  const int es = (int)((bits >> 52) & 0x7ff);
+  if (ea > 1 && eb > 1 && es > 1 && es < 0x7ff && ea < 0x7ff && eb < 0x7ff)
+    return __longlong_as_double(bits - (1ll << 52));
+  return 0.5 * a + 0.5 * b;
+}
 
 // Work record (depth, velocity) of a state whose depth w - z is `depth`
 // (protect and the preparation of the extrapolation, in FP32 on the depth
@@ -315,7 +330,7 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& w, double& 
   }
   if (Ek.w != 0.0f) { uh = 0.0; vh = 0.0; }
   const float uh32 = d2f_bits(uh), vh32 = d2f_bits(vh);
-  const float x = manning_x(P, fmaxf(h, 0.0f), uh32, vh32, eta, dt);
+  const float x = manning_x(P, fmaxf(h, 0.0f), uh32, vh32, eta, dt32);
   const float dw = dt32 * Ek.x;
   float du = dt32 * Ek.y;
   float dv = dt32 * Ek.z;
@@ -540,17 +555,17 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         const double z = zk;
         double depth1;
         neg = update_lean(P, w, uh, vh, z, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f), dt,
-                          (float)dt, added, depth1);
-        w = 0.5 * w + 0.5 * d.wA[k];
-        uh = 0.5 * uh + 0.5 * d.uhA[k];
-        vh = 0.5 * vh + 0.5 * d.vhA[k];
+                          S->clock.timestep32, added, depth1);
+        w = half_sum(w, d.wA[k]);
+        uh = half_sum(uh, d.uhA[k]);
+        vh = half_sum(vh, d.vhA[k]);
         d.wA[k] = w;
         d.uhA[k] = uh;
         d.vhA[k] = vh;
         d.W0[k] = record_of(P, w - z, uh, vh);     // work record of the next step
       }
       const float bs = block_sum_f(bfl, shf);
-      const int anym = __syncthreads_or(added != 0.0);
+      const int anym = __syncthreads_or(__double_as_longlong(added) != 0);
       const double ma = anym ? block_sum_d(added, shd) : 0.0;
       const int nneg = __syncthreads_count(neg);
       if (threadIdx.x == 0) {
@@ -587,7 +602,7 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     if (valid) {
       const double dt = S->clock.timestep;
       double depth1;
-      neg = update_lean(P, w, uh, vh, z, d.area + k, etak, Ek, dt, (float)dt, added, depth1);
+      neg = update_lean(P, w, uh, vh, z, d.area + k, etak, Ek, dt, S->clock.timestep32, added, depth1);
       const float4 r = record_of(P, depth1, uh, vh);
       if (euler) {
         d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh;
@@ -599,7 +614,7 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     }
     const unsigned full = 0xffffffffu;
     const unsigned nb = __ballot_sync(full, neg);
-    if (__any_sync(full, added != 0.0)) {
+    if (__any_sync(full, __double_as_longlong(added) != 0)) {
       const double ws = warp_sum_d(added);
       if ((threadIdx.x & 31) == 0 && ws != 0.0) atomicAdd(&S->clock.mass_added, ws);
     }
