@@ -18,8 +18,9 @@
 //            combine 0.5 q0 + 0.5 q2 and the work record of the next step
 //   rates  : Rate_operator stage changes
 //   clock  : per-scenario time bookkeeping; sets the graph's while condition
-// The conserved state (w, uh, vh) and the bed are FP64; the depth w - z is
-// formed in FP64 and rounded once; fluxes and reconstruction are FP32.
+// The conserved state is kept as (depth h = w - z, uh, vh) in FP64, so the
+// depth at wet/dry fronts needs no subtraction in the step; the stage w
+// exists only at the interface (set/get).  Fluxes and reconstruction are FP32.
 #include "agx_internal.cuh"
 #include "de_mixed.cuh"
 #include "../../include/agx_pool.h"
@@ -118,18 +119,17 @@ __device__ double block_sum_d(double x, double* sh) {
 // protect: sw_domain_openmp.c:1096-1171; preparation: :1373-1402.  Applies
 // the state changes to (w, uh, vh) and returns the work record and the mass
 // added.
-__device__ __forceinline__ float4 protect_prep(const MParams& P, double& w, double& uh, double& vh, double z,
+__device__ __forceinline__ float4 protect_prep(const MParams& P, double& h, double& uh, double& vh,
                                                double area, double& added) {
-  const double depth = w - z;
   added = 0.0;
-  if (depth < P.hmin64) {
+  if (h < P.hmin64) {
     uh = 0.0;
-    if (depth <= 0.0 && w < z) {
-      added = (z - w) * area;
-      w = z;
+    if (h < 0.0) {             // stage below the bed
+      added = -h * area;
+      h = 0.0;
     }
   }
-  const double dk = fmax(w - z, 0.0);
+  const double dk = fmax(h, 0.0);
   float4 r;
   r.x = (float)dk;
   r.w = 0.0f;
@@ -314,10 +314,8 @@ __device__ __forceinline__ float4 record_of(const MParams& P, double depth, doub
 // The increments dt*E (and the friction correction) are formed in FP32 and
 // accumulated into the FP64 state with one FP64 add per quantity.
 // Returns 1 if the cell was fixed as negative; depth1 = w - z afterwards.
-__device__ __forceinline__ int update_lean(const MParams& P, double& w, double& uh, double& vh, double z,
-                                           const double* area, float eta, float4 Ek, double dt, float dt32,
-                                           double& added, double& depth1) {
-  const double depth = w - z;
+__device__ __forceinline__ int update_lean(const MParams& P, double& depth, double& uh, double& vh,
+                                           const double* area, float eta, float4 Ek, float dt32, double& added) {
   const float h = d2f_bits(depth);
   added = 0.0;
   if (h <= P.hmin) {
@@ -325,7 +323,7 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& w, double& 
     vh = 0.0;
     if (negative_bits(depth)) {
       added = -depth * (*area);
-      w = z;
+      depth = 0.0;
     }
   }
   if (Ek.w != 0.0f) { uh = 0.0; vh = 0.0; }
@@ -336,15 +334,13 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& w, double& 
   float dv = dt32 * Ek.z;
   du = du - x * (uh32 + du);
   dv = dv - x * (vh32 + dv);
-  w = w + f2d_bits(dw);
+  depth = depth + f2d_bits(dw);
   uh = uh + f2d_bits(du);
   vh = vh + f2d_bits(dv);
-  depth1 = w - z;
-  if (negative_bits(depth1)) {
-    w = z;
+  if (negative_bits(depth)) {
+    depth = 0.0;
     uh = 0.0;
     vh = 0.0;
-    depth1 = 0.0;
     return 1;
   }
   return 0;
@@ -426,12 +422,11 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
     float ew = 0.f, ex = 0.f, ey = 0.f, smax = 0.f, bfl = 0.f;
     float4 g3 = make_float4(0.f, 0.f, 0.f, 0.f), g4 = g3;
     // the FP64 state of the fused update is loaded before the flux loop
-    double sw = 0.0, suh = 0.0, svh = 0.0, zk = 0.0;
+    double sw = 0.0, suh = 0.0, svh = 0.0;
     if (FUSED2 && valid) {
       sw = d.wB[k];
       suh = d.uhB[k];
       svh = d.vhB[k];
-      zk = d.z[k];
     }
     if (valid) {
       const float4 g2 = d.g2[k];
@@ -550,19 +545,16 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
       int neg = 0;
       double added = 0.0;
       if (valid) {
-        const double dt = S->clock.timestep;
-        double w = sw, uh = suh, vh = svh;
-        const double z = zk;
-        double depth1;
-        neg = update_lean(P, w, uh, vh, z, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f), dt,
-                          S->clock.timestep32, added, depth1);
-        w = half_sum(w, d.wA[k]);
+        double h = sw, uh = suh, vh = svh;
+        neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
+                          S->clock.timestep32, added);
+        h = half_sum(h, d.wA[k]);
         uh = half_sum(uh, d.uhA[k]);
         vh = half_sum(vh, d.vhA[k]);
-        d.wA[k] = w;
+        d.wA[k] = h;
         d.uhA[k] = uh;
         d.vhA[k] = vh;
-        d.W0[k] = record_of(P, w - z, uh, vh);     // work record of the next step
+        d.W0[k] = record_of(P, h, uh, vh);     // work record of the next step
       }
       const float bs = block_sum_f(bfl, shf);
       const int anym = __syncthreads_or(__double_as_longlong(added) != 0);
@@ -586,8 +578,7 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     const int k = tile * TILE + threadIdx.x;
     // the cell's data are loaded before the tile's scenario is known (every
     // index of a used tile lies inside the pool's arrays)
-    double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
-    const double z = d.z[k];
+    double h = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
     const float etak = d.eta[k];
     const float4 Ek = d.E[k];
     const int sid = d.tile_scn[tile];
@@ -600,15 +591,13 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     int neg = 0;
     double added = 0.0;
     if (valid) {
-      const double dt = S->clock.timestep;
-      double depth1;
-      neg = update_lean(P, w, uh, vh, z, d.area + k, etak, Ek, dt, S->clock.timestep32, added, depth1);
-      const float4 r = record_of(P, depth1, uh, vh);
+      neg = update_lean(P, h, uh, vh, d.area + k, etak, Ek, S->clock.timestep32, added);
+      const float4 r = record_of(P, h, uh, vh);
       if (euler) {
-        d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh;
+        d.wA[k] = h; d.uhA[k] = uh; d.vhA[k] = vh;
         d.W0[k] = r;
       } else {
-        d.wB[k] = w; d.uhB[k] = uh; d.vhB[k] = vh;
+        d.wB[k] = h; d.uhB[k] = uh; d.vhB[k] = vh;
         d.W1[k] = r;
       }
     }
@@ -635,9 +624,9 @@ __global__ void k_pool_prep(PoolDev d, int inplace, int only_scn) {
     const bool valid = k < S->cell0 + S->ncell;
     double added = 0.0;
     if (valid) {
-      double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
-      d.W0[k] = protect_prep(S->P, w, uh, vh, d.z[k], d.area[k], added);
-      if (inplace) { d.wA[k] = w; d.uhA[k] = uh; d.vhA[k] = vh; }
+      double h = d.wA[k], uh = d.uhA[k], vh = d.vhA[k];
+      d.W0[k] = protect_prep(S->P, h, uh, vh, d.area[k], added);
+      if (inplace) { d.wA[k] = h; d.uhA[k] = uh; d.vhA[k] = vh; }
     }
     const double ma = block_sum_d(added, shd);
     if (threadIdx.x == 0 && inplace && ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
@@ -737,7 +726,7 @@ __device__ __forceinline__ double rate_cell(const PoolDev& d, const PoolOp& op, 
     d.wA[k] = d.wA[k] + local;
     infl = local * d.area[k];
   } else {
-    const double height = d.wA[k] - d.z[k];
+    const double height = d.wA[k];
     const double local = fmax(op.factor * dt * op.rate, -height);
     const double f = local < 0.0 ? (local + height) / (height + 1.0e-10) : 1.0;
     d.wA[k] = d.wA[k] + local;
@@ -745,8 +734,8 @@ __device__ __forceinline__ double rate_cell(const PoolDev& d, const PoolOp& op, 
     d.vhA[k] = d.vhA[k] * f;
     infl = local * d.area[k];
   }
-  double w = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
-  d.W0[k] = protect_prep(S->P, w, uh, vh, d.z[k], d.area[k], added);
+  double h = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
+  d.W0[k] = protect_prep(S->P, h, uh, vh, d.area[k], added);
   return infl;
 }
 
@@ -800,9 +789,27 @@ __global__ void k_scatter_f(double* dst, const float* src, const int* order, int
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < n) dst[order[j]] = (double)src[j];
 }
-__global__ void k_scatter_height(double* dst, const double* w, const double* z, const int* order, int n) {
+__global__ void k_scatter_height(double* dst, const double* h, const int* order, int n) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < n) dst[order[j]] = fmax(w[j] - z[j], 0.0);
+  if (j < n) dst[order[j]] = fmax(h[j], 0.0);
+}
+// The pool's conserved state is (depth h = stage - bed, uh, vh) in FP64; the
+// stage exists only at the interface.
+__global__ void k_gather_depth(double* h, const double* z, const double* stage, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) h[j] = stage[order[j]] - z[j];
+}
+__global__ void k_gather_bed(double* h, double* z, const double* bed, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) {
+    const double zn = bed[order[j]];
+    h[j] = (h[j] + z[j]) - zn;
+    z[j] = zn;
+  }
+}
+__global__ void k_scatter_stage(double* dst, const double* h, const double* z, const int* order, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[order[j]] = h[j] + z[j];
 }
 __global__ void k_scatter_E(double* dst, const float4* E, int comp, const int* order, int n) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1345,6 +1352,10 @@ agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t f, const double* 
   PCK(cudaMemcpyAsync(p->staging, host, n * 8, cudaMemcpyHostToDevice, p->stream));
   if (f == AGX_FRICTION_C) {
     k_gather_f<<<nblk1((int)n), 256, 0, p->stream>>>(p->d.eta + c0, p->staging, sh.order, (int)n);
+  } else if (f == AGX_STAGE_C) {       // the pool keeps the depth stage - bed
+    k_gather_depth<<<nblk1((int)n), 256, 0, p->stream>>>(p->d.wA + c0, p->d.z + c0, p->staging, sh.order, (int)n);
+  } else if (f == AGX_ELEV_C) {        // a new bed keeps the stage
+    k_gather_bed<<<nblk1((int)n), 256, 0, p->stream>>>(p->d.wA + c0, p->d.z + c0, p->staging, sh.order, (int)n);
   } else {
     k_gather<<<nblk1((int)n), 256, 0, p->stream>>>(dst + c0, p->staging, sh.order, (int)n);
   }
@@ -1358,20 +1369,22 @@ agx_status agx_pool_set_field(agx_pool p, int32_t sid, int32_t f, const double* 
   return psync(p);
 }
 
-__global__ void k_gather3(double* w, double* uh, double* vh, const double* src, const int* order, int n) {
+__global__ void k_gather3(double* w, double* uh, double* vh, const double* z, const double* src, const int* order,
+                          int n) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < n) {
     const int o = order[j];
-    w[j] = src[o];
+    w[j] = src[o] - z[j];
     uh[j] = src[(size_t)n + o];
     vh[j] = src[2 * (size_t)n + o];
   }
 }
-__global__ void k_scatter3(double* dst, const double* w, const double* uh, const double* vh, const int* order, int n) {
+__global__ void k_scatter3(double* dst, const double* w, const double* uh, const double* vh, const double* z,
+                           const int* order, int n) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < n) {
     const int o = order[j];
-    dst[o] = w[j];
+    dst[o] = w[j] + z[j];
     dst[(size_t)n + o] = uh[j];
     dst[2 * (size_t)n + o] = vh[j];
   }
@@ -1392,22 +1405,22 @@ static bool host_mapped(const void* ptr) {
 
 // Direct exchange with mapped host buffers, walked in the caller's order
 // (contiguous on the host side; permuted on the device side).
-__global__ void k_state_from_host(double* w, double* uh, double* vh, const double* hw, const double* huh,
-                                  const double* hvh, const int* inv, int n) {
+__global__ void k_state_from_host(double* w, double* uh, double* vh, const double* z, const double* hw,
+                                  const double* huh, const double* hvh, const int* inv, int n) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o < n) {
     const int j = inv[o];
-    w[j] = hw[o];
+    w[j] = hw[o] - z[j];
     uh[j] = huh[o];
     vh[j] = hvh[o];
   }
 }
 __global__ void k_state_to_host(double* hw, double* huh, double* hvh, const double* w, const double* uh,
-                                const double* vh, const int* inv, int n) {
+                                const double* vh, const double* z, const int* inv, int n) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o < n) {
     const int j = inv[o];
-    hw[o] = w[j];
+    hw[o] = w[j] + z[j];
     huh[o] = uh[j];
     hvh[o] = vh[j];
   }
@@ -1425,8 +1438,8 @@ agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const do
   const int c0 = sh.tile0 * TILE;
   cudaStream_t st = p->stream;
   if (host_mapped(w) && host_mapped(uh) && host_mapped(vh)) {
-    k_state_from_host<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, w, uh, vh,
-                                                    sh.inv, (int)n);
+    k_state_from_host<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->d.z + c0, w, uh,
+                                                    vh, sh.inv, (int)n);
     count_launch();
     PCK(cudaGetLastError());
     sh.work_dirty = true;
@@ -1435,7 +1448,8 @@ agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const do
   PCK(cudaMemcpyAsync(p->staging, w, n * 8, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync(p->staging + n, uh, n * 8, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync(p->staging + 2 * n, vh, n * 8, cudaMemcpyHostToDevice, st));
-  k_gather3<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->staging, sh.order, (int)n);
+  k_gather3<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->d.z + c0, p->staging,
+                                           sh.order, (int)n);
   count_launch();
   PCK(cudaGetLastError());
   sh.work_dirty = true;
@@ -1450,13 +1464,14 @@ agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, do
   const int c0 = sh.tile0 * TILE;
   cudaStream_t st = p->stream;
   if (host_mapped(w) && host_mapped(uh) && host_mapped(vh)) {
-    k_state_to_host<<<nblk1((int)n), 256, 0, st>>>(w, uh, vh, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, sh.inv,
-                                                  (int)n);
+    k_state_to_host<<<nblk1((int)n), 256, 0, st>>>(w, uh, vh, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0,
+                                                  p->d.z + c0, sh.inv, (int)n);
     count_launch();
     PCK(cudaGetLastError());
     return psync(p);
   }
-  k_scatter3<<<nblk1((int)n), 256, 0, st>>>(p->staging, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, sh.order, (int)n);
+  k_scatter3<<<nblk1((int)n), 256, 0, st>>>(p->staging, p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->d.z + c0,
+                                            sh.order, (int)n);
   count_launch();
   PCK(cudaGetLastError());
   PCK(cudaMemcpyAsync(w, p->staging, n * 8, cudaMemcpyDeviceToHost, st));
@@ -1475,12 +1490,12 @@ agx_status agx_pool_get_field(agx_pool p, int32_t sid, int32_t f, double* host, 
   double* out = p->staging;
   cudaStream_t st = p->stream;
   switch (f) {
-    case AGX_STAGE_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, sh.order, N); break;
+    case AGX_STAGE_C: k_scatter_stage<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, p->d.z + c0, sh.order, N); break;
     case AGX_XMOM_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.uhA + c0, sh.order, N); break;
     case AGX_YMOM_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.vhA + c0, sh.order, N); break;
     case AGX_ELEV_C: k_scatter<<<nblk1(N), 256, 0, st>>>(out, p->d.z + c0, sh.order, N); break;
     case AGX_FRICTION_C: k_scatter_f<<<nblk1(N), 256, 0, st>>>(out, p->d.eta + c0, sh.order, N); break;
-    case AGX_HEIGHT_C: k_scatter_height<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, p->d.z + c0, sh.order, N); break;
+    case AGX_HEIGHT_C: k_scatter_height<<<nblk1(N), 256, 0, st>>>(out, p->d.wA + c0, sh.order, N); break;
     case AGX_MAX_SPEED: k_scatter_f<<<nblk1(N), 256, 0, st>>>(out, p->d.maxs + c0, sh.order, N); break;
     case AGX_STAGE_X: case AGX_XMOM_X: case AGX_YMOM_X:
       k_scatter_E<<<nblk1(N), 256, 0, st>>>(out, p->d.E + c0, f - AGX_STAGE_X, sh.order, N); break;

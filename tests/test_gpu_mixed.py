@@ -180,6 +180,17 @@ def test_snapshot_restore_and_autotune_leave_state_unchanged():
         assert np.array_equal(o, outs[0])
 
 
+def _same_state(got, want, d, name):
+    """Momenta come back bitwise; the stage is stored as depth (stage - bed),
+    so it comes back to within one rounding of the bed's magnitude."""
+    if name != "stage_c":
+        assert np.array_equal(got, want), name
+        return
+    z = d.quantities["elevation"].centroid_values
+    tol = 2.0 * np.finfo(float).eps * max(np.abs(want).max(), np.abs(z).max(), 1.0)
+    assert np.abs(got - want).max() <= tol, name
+
+
 def test_state_exchange_in_one_call_matches_per_field():
     d = workloads.dam_break(m=30, flow_algorithm="DE1", precision="mixed")
     for _ in d.evolve(yieldstep=0.5, finaltime=0.5):
@@ -192,7 +203,7 @@ def test_state_exchange_in_one_call_matches_per_field():
     w2, uh2, vh2 = w + 0.01 * rng.uniform(size=w.size), uh * 0.5, vh * 0.25
     scn.set_state(w2, uh2, vh2)
     for name, ref in (("stage_c", w2), ("xmom_c", uh2), ("ymom_c", vh2)):
-        assert np.array_equal(scn.get(name), ref), name
+        _same_state(scn.get(name), ref, d, name)
 
 
 def test_state_exchange_with_page_locked_buffers():
@@ -215,7 +226,7 @@ def test_state_exchange_with_page_locked_buffers():
         a[:] = b
     scn.set_state(*pin)
     for name, b in zip(("stage_c", "xmom_c", "ymom_c"), new):
-        assert np.array_equal(scn.get(name), b), name
+        _same_state(scn.get(name), b, d, name)
 
 
 def test_full_size_mixed_against_plain_fp64():
