@@ -23,6 +23,7 @@
 // exists only at the interface (set/get).  Fluxes and reconstruction are FP32.
 #include "agx_internal.cuh"
 #include "de_mixed.cuh"
+#include "inlet.cuh"
 #include "../../include/agx_pool.h"
 #include <algorithm>
 #include <cstdarg>
@@ -709,17 +710,24 @@ __global__ void k_pool_reset(PoolDev d, int nscn) {
   S->clock.bfs[1] = 0.0;
 }
 
+// A fractional-step operator of one scenario: Rate_operator (kind 0) or
+// Inlet_operator (kind 1: rate = the discharge Q, vu/vv the imposed velocity
+// when flags & 1, zero velocity when flags & 2, area = the inlet's area).
 struct PoolOp {
   int sid;
   const int* idx;    // pool cells
   int n;
   double rate, factor;
+  int kind = 0;
+  int flags = 0;
+  double vu = 0.0, vv = 0.0, area = 0.0;
+  double dt = -1.0;  // < 0: the step's timestep from the scenario's clock
 };
 
 // Rate_operator change of one cell of op's index set; returns the influx.
 __device__ __forceinline__ double rate_cell(const PoolDev& d, const PoolOp& op, PoolScn* S) {
   const int k = op.idx[threadIdx.x + blockIdx.x * blockDim.x];
-  const double dt = S->clock.timestep;
+  const double dt = op.dt >= 0.0 ? op.dt : S->clock.timestep;
   double infl;
   if (op.rate >= 0.0) {
     const double local = op.factor * dt * op.rate;
@@ -739,11 +747,13 @@ __device__ __forceinline__ double rate_cell(const PoolDev& d, const PoolOp& op, 
   return infl;
 }
 
-__global__ void __launch_bounds__(256) k_pool_rate(PoolDev d, PoolOp op, int slot) {
+// One application of a Rate_operator: inside the step loop (from_host 0)
+// only while the scenario is running; from the host after a step always.
+__global__ void __launch_bounds__(256) k_pool_rate(PoolDev d, PoolOp op, int slot, int from_host) {
   __shared__ double part[256 / 32];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   PoolScn* S = d.scn + op.sid;
-  if (!S->active) return;
+  if (!from_host && !S->active) return;
   double infl = 0.0;
   if (j < op.n) infl = rate_cell(d, op, S);
   // influx: one atomic per block (a single address receives every block's sum)
@@ -756,6 +766,46 @@ __global__ void __launch_bounds__(256) k_pool_rate(PoolDev d, PoolOp op, int slo
     r = warp_sum_d(r);
     if (lane == 0 && slot < MAX_OPS && r != 0.0) atomicAdd(&S->clock.op_influx[slot], r);
   }
+}
+
+// Inlet_operator on the pool's depth-stored state (steps in inlet.cuh).
+struct PoolInletCells {
+  PoolDev d;
+  const int* idx;
+  __device__ int cell(int a) const { return idx[a]; }
+  __device__ double stage(int k) const { return d.wA[k] + d.z[k]; }
+  __device__ double height(int k) const { return d.wA[k]; }
+  __device__ double area(int k) const { return d.area[k]; }
+  __device__ double uh(int k) const { return d.uhA[k]; }
+  __device__ double vh(int k) const { return d.vhA[k]; }
+  __device__ void set_level(int k, double level) { d.wA[k] = level - d.z[k]; }
+  __device__ void set_depth(int k, double depth) { d.wA[k] = depth; }
+  __device__ void empty(int k) {
+    d.wA[k] = 0.0;
+    d.uhA[k] = 0.0;
+    d.vhA[k] = 0.0;
+  }
+  __device__ void set_momenta(int k, double mx, double my) {
+    d.uhA[k] = mx;
+    d.vhA[k] = my;
+  }
+};
+
+// Discharge Q = 0.5 (q1 + q2) over the timestep (op.dt, or the clock's);
+// the changed cells' work records are formed again for the next step.
+__global__ void __launch_bounds__(INLET_TPB) k_pool_inlet(PoolDev d, PoolOp op, int slot, double q1, double q2,
+                                                          int from_host) {
+  PoolScn* S = d.scn + op.sid;
+  if (!from_host && !S->active) return;
+  const double dt = op.dt >= 0.0 ? op.dt : S->clock.timestep;
+  PoolInletCells c{d, op.idx};
+  const double applied = inlet_apply(c, op.n, op.flags, op.vu, op.vv, op.area, 0.5 * (q1 + q2) * dt);
+  for (int a = threadIdx.x; a < op.n; a += INLET_TPB) {
+    const int k = op.idx[a];
+    double h = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
+    d.W0[k] = protect_prep(S->P, h, uh, vh, d.area[k], added);
+  }
+  if (threadIdx.x == 0 && slot < MAX_OPS) S->clock.op_influx[slot] += applied;
 }
 
 // Per-scenario clocks (one thread each, one block); sets the graph's while
@@ -829,6 +879,7 @@ struct ScnHost {
   int* inv = nullptr;            // device [N]: stored index of each original cell
   double* series = nullptr;
   std::vector<PoolOp> ops;
+  bool host_ops = false;         // operators applied from the host after each step, not in the loop
   bool work_dirty = true;
   bool running = false;          // serving: still has steps to take towards its final time
 };
@@ -972,7 +1023,10 @@ static void init_clock_p(Clock* c, const agx_params& p) {
 
 static int nblk1(int n) { return (n + 255) / 256; }
 
-static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+// One step of every active scenario in two parts: the first stage (flux,
+// timestep, first update; Euler scenarios are complete after it), then the
+// second RK2 stage, the operators of the step loop and the clocks.
+static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   const PoolDev& d = p->d;
   const int S = p->cap_scn;
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
@@ -991,16 +1045,24 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   k_pool_update<<<std::max(d.ntiles, 1), TILE, 0, st>>>(d, 0);
   count_launch();
   phase_mark(st, PH_UPDATE);
+  return cudaGetLastError();
+}
+
+static cudaError_t enqueue_second_stage(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  const PoolDev& d = p->d;
+  const int S = p->cap_scn;
+  const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
   if (p->variant == 0) k_pool_flux<true, 6><<<Gf, TILE, 0, st>>>(d);
   else k_pool_flux<true, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
   for (size_t s = 0; s < p->scn.size(); s++) {
     const ScnHost& sh = p->scn[s];
-    if (!sh.alive) continue;
+    if (!sh.alive || sh.host_ops) continue;
     for (size_t i = 0; i < sh.ops.size(); i++) {
       const PoolOp& op = sh.ops[i];
-      k_pool_rate<<<nblk1(op.n), 256, 0, st>>>(d, op, (int)i);
+      if (op.kind == 1) k_pool_inlet<<<1, INLET_TPB, 0, st>>>(d, op, (int)i, op.rate, op.rate, 0);
+      else k_pool_rate<<<nblk1(op.n), 256, 0, st>>>(d, op, (int)i, 0);
       count_launch();
       phase_mark(st, PH_RATE);
     }
@@ -1009,6 +1071,12 @@ static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long lon
   count_launch();
   phase_mark(st, PH_SMALL);
   return cudaGetLastError();
+}
+
+static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  cudaError_t e = enqueue_first_stage(p, st);
+  if (e != cudaSuccess) return e;
+  return enqueue_second_stage(p, st, h, set_cond);
 }
 
 static agx_status pool_build_graph(Pool* p) {
@@ -1565,11 +1633,11 @@ agx_status agx_pool_set_boundary_series(agx_pool p, int32_t sid, const double* r
   return push_scn(p);
 }
 
-agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double rate, double factor) {
-  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+// Registers an operator over the caller's cell indices idx[n] (NULL: every
+// cell), mapped to pool cells on the host.
+static agx_status pool_add_op(Pool* p, int sid, const int32_t* idx, int64_t n, PoolOp op) {
   ScnHost& sh = p->scn[sid];
   if (sh.ops.size() >= (size_t)MAX_OPS) return pfail(AGX_E_INVALID, "at most %d operators", MAX_OPS);
-  // indices are in the caller's order: map them to pool cells on the host
   std::vector<int32_t> ord(sh.N);
   PCK(cudaMemcpyAsync(ord.data(), sh.order, sh.N * 4, cudaMemcpyDeviceToHost, p->stream));
   agx_status st = psync(p);
@@ -1580,13 +1648,15 @@ agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_
   const int c0 = sh.tile0 * TILE;
   if (idx) {
     for (int64_t i = 0; i < n; i++) {
-      if (idx[i] < 0 || idx[i] >= sh.N) return pfail(AGX_E_INVALID, "operator index out of range");
+      if (idx[i] < 0 || idx[i] >= sh.N) return pfail(AGX_E_INVALID, "operator index %d out of range", idx[i]);
       cells.push_back(inv[idx[i]] + c0);
     }
   } else {
     for (int j = 0; j < sh.N; j++) cells.push_back(c0 + j);
   }
-  PoolOp op{sid, nullptr, (int)cells.size(), rate, factor};
+  op.sid = sid;
+  op.idx = nullptr;
+  op.n = (int)cells.size();
   if (!cells.empty()) {
     int* dptr = nullptr;
     PCK(cudaMalloc(&dptr, cells.size() * 4));
@@ -1595,6 +1665,63 @@ agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_
   }
   sh.ops.push_back(op);
   p->graph_valid = false;
+  return psync(p);
+}
+
+agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double rate, double factor) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  PoolOp op{};
+  op.rate = rate;
+  op.factor = factor;
+  return pool_add_op(p, sid, idx, n, op);
+}
+
+agx_status agx_pool_add_inlet(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double Q, double area,
+                              int32_t flags, double velocity_u, double velocity_v) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  if (!idx || n <= 0) return pfail(AGX_E_INVALID, "an inlet needs at least one cell");
+  if (n > INLET_MAX) return pfail(AGX_E_INVALID, "an inlet region holds at most %d cells, got %lld", INLET_MAX,
+                                  (long long)n);
+  if (!(area > 0.0)) return pfail(AGX_E_INVALID, "inlet area must be positive");
+  PoolOp op{};
+  op.rate = Q;
+  op.factor = 1.0;
+  op.kind = 1;
+  op.flags = flags;
+  op.vu = velocity_u;
+  op.vv = velocity_v;
+  op.area = area;
+  return pool_add_op(p, sid, idx, n, op);
+}
+
+agx_status agx_pool_operators_from_host(agx_pool p, int32_t sid, int32_t on) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  if (p->scn[sid].host_ops != (on != 0)) p->graph_valid = false;
+  p->scn[sid].host_ops = on != 0;
+  return AGX_OK;
+}
+
+agx_status agx_pool_apply_operator(agx_pool p, int32_t sid, int32_t op, double rate, double factor,
+                                   double timestep) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (op < 0 || op >= (int)sh.ops.size() || !(timestep >= 0.0))
+    return pfail(AGX_E_INVALID, "bad operator %d or timestep", op);
+  agx_status st = ensure_work(p, sid);
+  if (st) return st;
+  PoolOp o = sh.ops[op];
+  o.dt = timestep;
+  if (o.n > 0) {
+    if (o.kind == 1) {
+      k_pool_inlet<<<1, INLET_TPB, 0, p->stream>>>(p->d, o, op, rate, factor, 1);
+    } else {
+      o.rate = rate;
+      o.factor = factor;
+      k_pool_rate<<<nblk1(o.n), 256, 0, p->stream>>>(p->d, o, op, 1);
+    }
+    count_launch();
+    PCK(cudaGetLastError());
+  }
   return psync(p);
 }
 
@@ -1685,6 +1812,28 @@ agx_status agx_pool_advance(agx_pool p, int32_t* n_done) {
     if (p->scn_host[s].clock.reason) done++;
   }
   count_launch(iters * p->kernels_per_iter);
+  if (n_done) *n_done = done;
+  return AGX_OK;
+}
+
+// One step split at the RK2 stages, without the graph (boundary values the
+// host evaluates at the second stage's time go in between).
+agx_status agx_pool_step_begin(agx_pool p) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
+  PCK(enqueue_first_stage(p, p->stream));
+  return psync(p);
+}
+
+agx_status agx_pool_step_end(agx_pool p, int32_t* n_done) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  PCK(enqueue_second_stage(p, p->stream, 0ull, false));
+  agx_status st = pull_scn(p);
+  if (st) return st;
+  int done = 0;
+  for (int s = 0; s < p->cap_scn; s++)
+    if (p->scn_host[s].alive && p->scn_host[s].clock.reason) done++;
   if (n_done) *n_done = done;
   return AGX_OK;
 }

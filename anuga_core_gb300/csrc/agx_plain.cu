@@ -11,6 +11,7 @@
 // All state stays in device memory; the clock kernel decides on the device
 // whether another step is needed and sets the graph's while condition.
 #include "agx_internal.cuh"
+#include "inlet.cuh"
 #include <cuda_runtime.h>
 
 namespace agx {
@@ -343,185 +344,38 @@ __global__ void k_rate(Dev d, const int* idx, int n, double rate, double factor,
   }
 }
 
-// Inlet_operator (structures/inlet_operator.py:75-165, inlet.py:107-226):
-// one block of 1024 threads for an inlet of n <= INLET_MAX cells.  The
+// Inlet_operator (structures/inlet_operator.py:75-165, inlet.py:107-226) on
+// the scenario's stage-stored state; the steps are in inlet.cuh.  The
 // discharge is Q = 0.5 (q1 + q2) over the timestep (dt_arg < 0: the step's
-// timestep from the clock).  A positive volume fills the lowest cells first
-// to a level surface (stages sorted, cumulative areas and volumes); a
-// negative one lowers all cells to one depth, or empties them.  Momenta are
-// depth x the cells' previous velocity (or the imposed one, or zero).
-constexpr int INLET_TPB = 1024;
-constexpr int INLET_PER = INLET_MAX / INLET_TPB;
-
-__device__ double inlet_block_sum(double x, double* part) {
-  x = warp_sum(x);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) part[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    double r = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
-    r = warp_sum(r);
-    if (lane == 0) part[0] = r;
+// timestep from the clock).
+struct PlainInletCells {
+  Dev d;
+  __device__ int cell(int a) const { return d_idx[a]; }
+  __device__ double stage(int k) const { return d.w[k]; }
+  __device__ double height(int k) const { return d.w[k] - d.z[k]; }
+  __device__ double area(int k) const { return d.areas[k]; }
+  __device__ double uh(int k) const { return d.uh[k]; }
+  __device__ double vh(int k) const { return d.vh[k]; }
+  __device__ void set_level(int k, double level) { d.w[k] = level; }
+  __device__ void set_depth(int k, double depth) { d.w[k] = d.z[k] + depth; }
+  __device__ void empty(int k) {
+    d.w[k] = d.z[k];
+    d.uh[k] = 0.0;
+    d.vh[k] = 0.0;
   }
-  __syncthreads();
-  const double r = part[0];
-  __syncthreads();
-  return r;
-}
-
-// Exclusive prefix sum of v[0..INLET_MAX) in place (INLET_PER consecutive
-// values per thread, then a scan of the per-thread totals).
-__device__ void inlet_exclusive_scan(double* v, double* part) {
-  const int t = threadIdx.x;
-  double run = 0.0;
-  double loc[INLET_PER];
-#pragma unroll
-  for (int j = 0; j < INLET_PER; j++) {
-    loc[j] = run;
-    run += v[t * INLET_PER + j];
+  __device__ void set_momenta(int k, double mx, double my) {
+    d.uh[k] = mx;
+    d.vh[k] = my;
   }
-  // inclusive scan of the thread totals across the block
-  double x = run;
-  const int lane = t & 31, wid = t >> 5;
-  for (int o = 1; o < 32; o <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) part[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    double w = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0;
-    for (int o = 1; o < 32; o <<= 1) {
-      const double y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    part[lane] = w;
-  }
-  __syncthreads();
-  const double before = (wid > 0 ? part[wid - 1] : 0.0) + (x - run);
-#pragma unroll
-  for (int j = 0; j < INLET_PER; j++) v[t * INLET_PER + j] = before + loc[j];
-  __syncthreads();
-}
+  const int* d_idx;
+};
 
 __global__ void __launch_bounds__(INLET_TPB) k_inlet(Dev d, RateOp op, int slot, double q1, double q2, double dt_arg) {
-  __shared__ double key[INLET_MAX];     // stages, sorted
-  __shared__ int pos[INLET_MAX];        // inlet position of each sorted stage
-  __shared__ double acc[INLET_MAX];     // cumulative areas / volumes
-  __shared__ double part[INLET_TPB / 32];
-  __shared__ int last;
-  const int n = op.n, t = threadIdx.x;
   const double dt = dt_arg >= 0.0 ? dt_arg : d.clock->timestep;
   const double volume = 0.5 * (q1 + q2) * dt;
-  double u[INLET_PER], v[INLET_PER], cur = 0.0;
-#pragma unroll
-  for (int j = 0; j < INLET_PER; j++) {
-    const int a = t + j * INLET_TPB;
-    u[j] = v[j] = 0.0;
-    if (a < n) {
-      const int k = op.idx[a];
-      const double h = d.w[k] - d.z[k];
-      cur += h * d.areas[k];
-      u[j] = d.uh[k] * h / (h * h + 1.0e-6);
-      v[j] = d.vh[k] * h / (h * h + 1.0e-6);
-      key[a] = d.w[k];
-      pos[a] = a;
-    } else {
-      key[a] = INFINITY;
-      pos[a] = a;
-    }
-  }
-  const double current = inlet_block_sum(cur, part);
-  double applied = volume;
-  if (volume >= 0.0) {
-    // bitonic sort of (stage, position) over INLET_MAX slots
-    for (int size = 2; size <= INLET_MAX; size <<= 1) {
-      for (int stride = size >> 1; stride > 0; stride >>= 1) {
-        __syncthreads();
-        for (int a = t; a < INLET_MAX; a += INLET_TPB) {
-          const int b = a ^ stride;
-          if (b > a) {
-            const bool up = (a & size) == 0;
-            const double ka = key[a], kb = key[b];
-            if ((ka > kb) == up) {
-              key[a] = kb;
-              key[b] = ka;
-              const int pa = pos[a];
-              pos[a] = pos[b];
-              pos[b] = pa;
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // cumulative areas of the cells ordered by stage
-    for (int a = t; a < INLET_MAX; a += INLET_TPB) acc[a] = a < n ? d.areas[op.idx[pos[a]]] : 0.0;
-    __syncthreads();
-    inlet_exclusive_scan(acc, part);
-    double sa[INLET_PER];
-#pragma unroll
-    for (int j = 0; j < INLET_PER; j++) {
-      const int a = t * INLET_PER + j;
-      sa[j] = acc[a] + (a < n ? d.areas[op.idx[pos[a]]] : 0.0);     // inclusive
-    }
-    __syncthreads();
-    // volume needed to fill the cells below sorted position a to its stage
-#pragma unroll
-    for (int j = 0; j < INLET_PER; j++) {
-      const int a = t * INLET_PER + j;
-      acc[a] = (a + 1 < n) ? sa[j] * (key[a + 1] - key[a]) : 0.0;
-    }
-    __syncthreads();
-    inlet_exclusive_scan(acc, part);
-    if (t == 0) last = 0;
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < INLET_PER; j++) {
-      const int a = t * INLET_PER + j;
-      if (a < n && acc[a] <= volume) atomicMax(&last, a);
-    }
-    __syncthreads();
-    const int index = last;
-    // inclusive cumulative area at `index`
-    if (t == index / INLET_PER) part[0] = sa[index % INLET_PER];
-    __syncthreads();
-    const double depth = (volume - acc[index]) / part[0];
-    const double level = key[index] + depth;
-    for (int a = t; a < n; a += INLET_TPB)
-      if (a <= index) d.w[op.idx[pos[a]]] = level;
-  } else if (current + volume >= 0.0) {
-    const double depth = (current + volume) / op.area;
-    for (int a = t; a < n; a += INLET_TPB) {
-      const int k = op.idx[a];
-      d.w[k] = d.z[k] + depth;
-    }
-  } else {
-    for (int a = t; a < n; a += INLET_TPB) {
-      const int k = op.idx[a];
-      d.w[k] = d.z[k];
-      d.uh[k] = 0.0;
-      d.vh[k] = 0.0;
-    }
-    applied = -current;
-  }
-  __syncthreads();
-  if (!(volume < 0.0 && current + volume < 0.0)) {
-#pragma unroll
-    for (int j = 0; j < INLET_PER; j++) {
-      const int a = t + j * INLET_TPB;
-      if (a < n) {
-        const int k = op.idx[a];
-        const double h = d.w[k] - d.z[k];
-        double mx = h * u[j], my = h * v[j];
-        if (op.flags & 1) { mx = h * op.vu; my = h * op.vv; }
-        if (op.flags & 2) { mx = 0.0; my = 0.0; }
-        d.uh[k] = mx;
-        d.vh[k] = my;
-      }
-    }
-  }
-  if (t == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
+  PlainInletCells c{d, op.idx};
+  const double applied = inlet_apply(c, op.n, op.flags, op.vu, op.vv, op.area, volume);
+  if (threadIdx.x == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
 }
 
 // One sww frame (file/sww.py:352-368 store_timestep with smoothed vertex

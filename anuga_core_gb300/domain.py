@@ -483,8 +483,6 @@ class Domain:
             if hasattr(op, "rate"):
                 self._scn.add_rate(op.indices, op.get_rate(t), op.get_factor(t))
             elif hasattr(op, "update_Q"):
-                if not hasattr(self._scn, "add_inlet"):
-                    raise NotImplementedError("Inlet_operator runs on the plain FP64 form (precision='fp64')")
                 self._scn.add_inlet(op.indices, op.update_Q(t), op.area, op.flags,
                                     op.velocity if op.velocity is not None else (0.0, 0.0))
             else:
@@ -636,6 +634,9 @@ class Domain:
         rf = self.relative_finaltime if getattr(self, "relative_finaltime", None) is not None else -1.0
         scn.set_clock(self.relative_time, self.relative_yieldtime, rf)
         st = scn.advance(max_steps)
+        return self._take_stats(st)
+
+    def _take_stats(self, st):
         self._mark_device_newer()
         self.relative_time = st.time
         self.timestep = st.last_timestep
@@ -649,7 +650,40 @@ class Domain:
         self._last_stats = st
         return st.reason
 
+    def _host_step_mixed(self):
+        """One step of the mixed form when a boundary or an operator is a
+        Python function of time: boundary values evaluated at the step's start
+        time for the first stage and at t + dt for the second RK2 stage (as
+        generic_domain.py:1974-2051), then every operator applied in
+        registration order with the step's timestep, at the time the
+        reference's operators see (the step's start for Euler, its end for
+        RK2)."""
+        if any(f is not manning_friction_implicit for f in self.forcing_terms):
+            raise NotImplementedError("the mixed form applies Manning friction only; other forcing terms run "
+                                      "on precision='fp64'")
+        scn = self._scn
+        t0 = self.relative_time
+        self._push_dirty()
+        host_bc = any(B is not None and not getattr(B, "device_loop", True) for B in self.boundary_map.values())
+        if host_bc:
+            self._bind_boundaries(self.get_time())
+        rf = self.relative_finaltime if getattr(self, "relative_finaltime", None) is not None else -1.0
+        scn.set_clock(t0, self.relative_yieldtime, rf)
+        dt = scn.step_begin()
+        if host_bc and self.timestepping_method != "euler":
+            self._bind_boundaries(self.starttime + t0 + dt)
+        reason = self._take_stats(scn.step_end())
+        t1 = self.relative_time
+        if self.timestepping_method == "euler":
+            self.relative_time = t0
+        for op in self.fractional_step_operators:
+            op()
+        self.relative_time = t1
+        return 0 if reason == _lib.STOP_MAXSTEPS else reason
+
     def _host_step(self, yieldstep, finaltime):
+        if self.precision == "mixed":
+            return self._host_step_mixed()
         t0 = self.relative_time
         if self.timestepping_method == "euler":
             self.evolve_one_euler_step(yieldstep, finaltime)
@@ -738,6 +772,8 @@ class Domain:
             self._pull(_STATE_FIELDS)
             yield self.get_time()
         device_loop = self._device_loop_ok()
+        if self.precision == "mixed":
+            self._scn.operators_from_host(not device_loop)
         while True:
             if device_loop:
                 reason = self._device_steps()

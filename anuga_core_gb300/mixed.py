@@ -45,12 +45,19 @@ def lib():
             "agx_pool_set_boundary_series": ([H, ctypes.c_int32, _f64p, ctypes.c_int64], ctypes.c_int32),
             "agx_pool_add_rate": ([H, ctypes.c_int32, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double],
                                   ctypes.c_int32),
+            "agx_pool_add_inlet": ([H, ctypes.c_int32, _i32p, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int32, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
+            "agx_pool_operators_from_host": ([H, ctypes.c_int32, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_apply_operator": ([H, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double], ctypes.c_int32),
             "agx_pool_clear_operators": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_set_clock": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int64], ctypes.c_int32),
             "agx_pool_deactivate": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_advance": ([H, P(ctypes.c_int32)], ctypes.c_int32),
+            "agx_pool_step_begin": ([H], ctypes.c_int32),
+            "agx_pool_step_end": ([H, P(ctypes.c_int32)], ctypes.c_int32),
             "agx_pool_get_stats": ([H, ctypes.c_int32, P(_lib.StepStats)], ctypes.c_int32),
             "agx_pool_operator_influx": ([H, ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
             "agx_pool_time_phases": ([H, ctypes.c_int32, _f64p, ctypes.c_int32], ctypes.c_int32),
@@ -178,6 +185,19 @@ class Pool:
             check(self.L.agx_pool_add_rate(self.h, sid, idx.ctypes.data_as(_i32p), idx.size, float(rate),
                                            float(factor)))
 
+    def add_inlet(self, sid, indices, Q, area, flags=0, velocity=(0.0, 0.0)):
+        idx = np.ascontiguousarray(indices, np.int32)
+        check(self.L.agx_pool_add_inlet(self.h, sid, idx.ctypes.data_as(_i32p), idx.size, float(Q), float(area),
+                                        int(flags), float(velocity[0]), float(velocity[1])))
+
+    def operators_from_host(self, sid, on=True):
+        """Leave the scenario's operators out of the step loop; the caller
+        applies them after each step with apply_operator."""
+        check(self.L.agx_pool_operators_from_host(self.h, sid, 1 if on else 0))
+
+    def apply_operator(self, sid, op, rate, factor, timestep):
+        check(self.L.agx_pool_apply_operator(self.h, sid, int(op), float(rate), float(factor), float(timestep)))
+
     def clear_operators(self, sid):
         check(self.L.agx_pool_clear_operators(self.h, sid))
 
@@ -199,6 +219,17 @@ class Pool:
     def advance(self):
         n = ctypes.c_int32()
         check(self.L.agx_pool_advance(self.h, ctypes.byref(n)))
+        return n.value
+
+    def step_begin(self):
+        """First stage of one step of every active scenario (see step_end)."""
+        check(self.L.agx_pool_step_begin(self.h))
+
+    def step_end(self):
+        """Second RK2 stage, step-loop operators and clocks; returns the
+        number of scenarios whose clock stopped."""
+        n = ctypes.c_int32()
+        check(self.L.agx_pool_step_end(self.h, ctypes.byref(n)))
         return n.value
 
     def stats(self, sid):
@@ -308,6 +339,15 @@ class MixedScenario:
     def add_rate(self, indices, rate, factor=1.0):
         self.pool.add_rate(self.sid, indices, rate, factor)
 
+    def add_inlet(self, indices, Q, area, flags=0, velocity=(0.0, 0.0)):
+        self.pool.add_inlet(self.sid, indices, Q, area, flags, velocity)
+
+    def operators_from_host(self, on=True):
+        self.pool.operators_from_host(self.sid, on)
+
+    def apply_operator(self, op, rate, factor, timestep):
+        self.pool.apply_operator(self.sid, op, rate, factor, timestep)
+
     def clear_operators(self):
         self.pool.clear_operators(self.sid)
 
@@ -337,6 +377,18 @@ class MixedScenario:
         t, y, f = getattr(self, "_clock", (0.0, 1e300, -1.0))
         self.pool.set_clock(self.sid, t, y, f, max_steps)
         self.pool.advance()
+        return self.pool.stats(self.sid)
+
+    def step_begin(self):
+        """One step (set_clock first) up to the end of its first stage;
+        returns the step's timestep."""
+        t, y, f = getattr(self, "_clock", (0.0, 1e300, -1.0))
+        self.pool.set_clock(self.sid, t, y, f, 1)
+        self.pool.step_begin()
+        return self.pool.stats(self.sid).last_timestep
+
+    def step_end(self):
+        self.pool.step_end()
         return self.pool.stats(self.sid)
 
     def stats(self):

@@ -66,6 +66,22 @@ agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, c
 agx_status agx_pool_set_boundary_series(agx_pool p, int32_t sid, const double* rows, int64_t n_rows);
 /* Rate_operator with a constant rate (operators/rate_operators.py:149-258). */
 agx_status agx_pool_add_rate(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double rate, double factor);
+/* Inlet_operator (structures/inlet_operator.py:17-165, inlet.py:107-226):
+ * discharge Q (m^3/s) into the cells idx[n] (at most 2048) of total area
+ * `area`; flags & 1: momenta from (velocity_u, velocity_v); flags & 2: zero
+ * velocity.  Same meaning as agx_add_inlet_operator. */
+agx_status agx_pool_add_inlet(agx_pool p, int32_t sid, const int32_t* idx, int64_t n, double Q, double area,
+                              int32_t flags, double velocity_u, double velocity_v);
+/* on != 0: the scenario's operators are left out of the step loop and the
+ * caller applies them after each step with agx_pool_apply_operator (rates,
+ * factors or discharges that are functions of time, evaluated by the host). */
+agx_status agx_pool_operators_from_host(agx_pool p, int32_t sid, int32_t on);
+/* One application of registered operator `op` (registration order) with the
+ * caller's values and timestep: a Rate_operator's rate and factor, an
+ * Inlet_operator's Q(t) and Q(t + timestep).  Same meaning as
+ * agx_apply_operator. */
+agx_status agx_pool_apply_operator(agx_pool p, int32_t sid, int32_t op, double rate, double factor,
+                                   double timestep);
 agx_status agx_pool_clear_operators(agx_pool p, int32_t sid);
 agx_status agx_pool_operator_influx(agx_pool p, int32_t sid, int32_t op, double* influx);
 /* distribute_to_vertices_and_edges (shallow_water_domain.py:1879-1915). */
@@ -79,6 +95,15 @@ agx_status agx_pool_deactivate(agx_pool p, int32_t sid);
 /* Step loop (generic_domain.py:1835-1912) for every active scenario until
  * each reaches its yield time, final time or step target; one graph launch. */
 agx_status agx_pool_advance(agx_pool p, int32_t* n_done);
+/* One step of every active scenario in two calls, without the graph, for
+ * boundary values the host evaluates at each RK2 stage's time
+ * (generic_domain.py:1974-2051 updates the boundary at t and at t + dt):
+ * agx_pool_step_begin runs the first stage (flux, timestep, first update;
+ * Euler scenarios are complete after it), after which agx_pool_get_stats
+ * gives each scenario's timestep; agx_pool_step_end runs the second stage,
+ * the operators of the step loop and the clocks. */
+agx_status agx_pool_step_begin(agx_pool p);
+agx_status agx_pool_step_end(agx_pool p, int32_t* n_done);
 /* Continuous batching: up to max_steps more steps for every running scenario,
  * launched without waiting; agx_pool_wait completes it. */
 agx_status agx_pool_launch_chunk(agx_pool p, int64_t max_steps);
