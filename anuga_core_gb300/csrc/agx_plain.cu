@@ -260,7 +260,7 @@ __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int 
     if (!update_quantity(w, d.xw[k], sw, dt)) bad = 1;
     if (!update_quantity(uh, d.xuh[k], suh, dt)) bad = 1;
     if (!update_quantity(vh, d.xvh[k], svh, dt)) bad = 1;
-    if ((w - z < 0.0) & (meta_full(d.conn[k].w) > 0)) {
+    if ((dkey(w - z) < -1) & (meta_full(d.conn[k].w) > 0)) {     // w - z < 0
       neg = 1;
       w = z;
       uh = 0.0;
