@@ -280,6 +280,7 @@ agx_status agx_scenario_create(const agx_mesh_desc* m, const agx_params* p, agx_
   P.low_froude = p->low_froude;
   P.protect_zero_ymom = p->protect_zero_ymom;
   P.sloped_mannings = p->use_sloped_mannings;
+  finish_params(P);
   s->d.N = s->N;
   s->d.B = s->B;
   s->d.E = s->E;

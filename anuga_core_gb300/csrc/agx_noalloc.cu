@@ -280,6 +280,7 @@ extern "C" agx_status agx_compute_fluxes_noalloc(const agx_params* p, const agx_
   P.low_froude = p->low_froude;
   P.protect_zero_ymom = p->protect_zero_ymom;
   P.sloped_mannings = p->use_sloped_mannings;
+  finish_params(P);
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   k_na_reset<<<1, 1, 0, s>>>(scr);

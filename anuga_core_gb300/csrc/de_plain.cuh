@@ -52,8 +52,8 @@ namespace agx {
 // ---- FP64 comparisons on the integer pipe ---------------------------------
 // For x not NaN, dkey(x) = bits ^ ((bits >> 63) logical>> 1) increases
 // strictly with x, except that -0 (key -1) sorts just below +0 (key 0); the
-// comparisons treat the two zeros as equal, as IEEE comparison does.  dmax
-// and dmin return +0 for a pair of opposite zeros.
+// comparisons treat the two zeros as equal, as IEEE comparison does.  For a
+// pair of opposite zeros dmax returns +0 and dmin -0.
 AGX_HD int64_t dbits(double x) {
 #ifdef __CUDA_ARCH__
   return __double_as_longlong(x);
@@ -109,7 +109,25 @@ struct Params {
   int low_froude;
   int protect_zero_ymom;        // 1: both momenta (sw_domain_orig.c), 0: xmom only (openmp)
   int sloped_mannings;
+  // betas at wet/dry factor 1 (beta_dry + (beta - beta_dry) * 1.0) and the
+  // reciprocals the limiter needs, formed once by finish_params (0: not
+  // positive, divided out per cell)
+  double beta_w1, beta_uh1, beta_vh1;
+  double inv_beta_w1, inv_beta_uh1, inv_beta_vh1, inv_beta_w;
 };
+
+AGX_HD double positive_inverse(double b) { return b > 0.0 ? 1.0 / b : 0.0; }
+
+// Derived parameters, with the device's operations.
+AGX_HD void finish_params(Params& P) {
+  P.beta_w1 = P.beta_w_dry + (P.beta_w - P.beta_w_dry) * 1.0;
+  P.beta_uh1 = P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * 1.0;
+  P.beta_vh1 = P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * 1.0;
+  P.inv_beta_w1 = positive_inverse(P.beta_w1);
+  P.inv_beta_uh1 = positive_inverse(P.beta_uh1);
+  P.inv_beta_vh1 = positive_inverse(P.beta_vh1);
+  P.inv_beta_w = positive_inverse(P.beta_w);
+}
 
 // ---- protect + depth/velocity preparation --------------------------------
 // Combines _openmp_protect (:1096-1171) with the first loop of the
@@ -164,12 +182,17 @@ AGX_HD double prep_cell(const Params& P, int k, double* w, double* uh, double* v
 
 // ---- limited reconstruction ----------------------------------------------
 // __limit_gradient (:1195-1231).  `lo`/`hi` are the admissible jump range.
-AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double beta) {
+// inv_known > 0 is 1/beta, formed beforehand; otherwise it is divided out.
+AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double beta, double inv_known) {
   const double tiny = 1.0e-100;
-  // Fast exact path: if every active ratio provably gives r*beta >= 1 the
-  // result of fmin(r*beta, 1) is decided without dividing.  A ratio hi/d
-  // with d > tiny satisfies fl(fl(hi/d)*beta) >= 1 whenever
-  // hi >= d * (1/beta) * (1 + 2^-40): the margin dwarfs the three roundings.
+  // The reference's phi = fmin(fmin(floor, r_0, r_1, r_2) * beta, 1) over the
+  // active ratios r_i (lo or hi over jump_i), floor = 1 if slot 0 is
+  // inactive, else 1000.  A ratio hi/d with d > tiny satisfies
+  // fl(fl(hi/d)*beta) >= 1 whenever hi >= d * (1/beta) * (1 + 2^-40) (the
+  // margin dwarfs the three roundings): such a ratio "passes".  A passing
+  // ratio can only be the minimum when phi is 1 whichever ratio is taken,
+  // so only the failing ratios are divided out; with none failing and
+  // floor*beta >= 1, phi is 1 without a division.
   const int64_t kneg = dkey(-tiny), kpos = dkey(tiny);
   bool neg[3], pos[3];
   for (int i = 0; i < 3; i++) {
@@ -177,23 +200,21 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
     neg[i] = kj < kneg;            // jump < -tiny
     pos[i] = kj > kpos;            // jump > tiny
   }
-  bool decided = dgt0(beta);
-  double ratio_floor = 1000.0;           // value of r if no ratio is below it
-  if (!neg[0] && !pos[0]) ratio_floor = 1.0;     // r0 keeps its initial 1.0
-  if (decided) {
-    const double inv_beta = 1.0 / beta;
+  const double ratio_floor = (!neg[0] && !pos[0]) ? 1.0 : 1000.0;
+  if (dgt0(beta)) {
+    const double inv_beta = dgt0(inv_known) ? inv_known : 1.0 / beta;
     const double need = inv_beta * (1.0 + 9.094947017729282e-13);
+    bool fail[3], any = false;
     for (int i = 0; i < 3; i++) {
       // ratio lo/d with both negative: lo/d >= need  <=>  lo <= d*need
-      if (neg[i] && !dle(lo, jump[i] * need)) decided = false;
-      else if (pos[i] && !dge(hi, jump[i] * need)) decided = false;
+      fail[i] = neg[i] ? !dle(lo, jump[i] * need) : (pos[i] && !dge(hi, jump[i] * need));
+      any |= fail[i];
     }
-    if (decided && !dle(inv_beta, ratio_floor)) decided = false;  // beta*floor may be < 1
-  }
-  if (decided) {
-    // every active ratio r_i satisfies r_i*beta >= 1 after rounding, so
-    // phi = fmin(min(r_i, floor)*beta, 1): if floor*beta >= 1 it is 1.
-    return dmin(ratio_floor * beta, 1.0);
+    if (!any && dle(inv_beta, ratio_floor)) return dmin(ratio_floor * beta, 1.0);
+    double r = ratio_floor;
+    for (int i = 0; i < 3; i++)
+      if (fail[i]) r = dmin((neg[i] ? lo : hi) / jump[i], r);
+    return dmin(r * beta, 1.0);
   }
   double r = 1000.0, cand = 1.0;
   for (int i = 0; i < 3; i++) {
@@ -211,7 +232,7 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
 //   nb==2 : g[6]=gradient factor x, g[7]=gradient factor y
 constexpr int GEO_STRIDE = 11;
 
-AGX_HD void reconstruct3(double beta, double qc, double q0, double q1, double q2,
+AGX_HD void reconstruct3(double beta, double inv_known, double qc, double q0, double q1, double q2,
                          const double* G, double out[3]) {
   if (!dgt0(beta)) {
     out[0] = qc; out[1] = qc; out[2] = qc;
@@ -228,11 +249,12 @@ AGX_HD void reconstruct3(double beta, double qc, double q0, double q1, double q2
   for (int i = 0; i < 3; i++) jump[i] = gx * G[i] + gy * G[3 + i];
   const double hi = dmax(dmax(d0, dmax(d0 + d1, d0 + d2)), 0.0);
   const double lo = dmin(dmin(d0, dmin(d0 + d1, d0 + d2)), 0.0);
-  const double phi = limiter_phi(jump, lo, hi, beta);
+  const double phi = limiter_phi(jump, lo, hi, beta, inv_known);
   for (int i = 0; i < 3; i++) out[i] = qc + jump[i] * phi;
 }
 
-AGX_HD void reconstruct_towards(double beta, double qc, double qn, const double* G, double out[3]) {
+AGX_HD void reconstruct_towards(double beta, double inv_known, double qc, double qn, const double* G,
+                                double out[3]) {
   const double d = qn - qc;
   const double gx = d * G[6];
   const double gy = d * G[7];
@@ -240,7 +262,7 @@ AGX_HD void reconstruct_towards(double beta, double qc, double qn, const double*
   for (int i = 0; i < 3; i++) jump[i] = gx * G[i] + gy * G[3 + i];
   double lo, hi;
   if (dge0(d)) { lo = 0.0; hi = d; } else { lo = d; hi = 0.0; }
-  const double phi = limiter_phi(jump, lo, hi, beta);
+  const double phi = limiter_phi(jump, lo, hi, beta, inv_known);
   for (int i = 0; i < 3; i++) out[i] = qc + jump[i] * phi;
 }
 
@@ -252,12 +274,16 @@ AGX_HD double wet_dry_factor(const Params& P, double hc, double hlo, double hhi)
   const double hhi_e = dmax(hhi, 1.0e-06);
   // A = c*max(hlo,0)/hc_e + d >= 1  <=>  hlo/hc_e >= (1-d)/c = 0.3 (a_tmp)
   // B = c*max(hc,0)/hhi_e + d >= 1 ; C = 1.2*(hlo-hmin)/(hlo+hmin) >= 1
-  if (dgt0(hlo) && dge(hlo, 0.30000000000000004 * hc_e * m) && dge(hc, 0.30000000000000004 * hhi_e * m) &&
-      dge(1.2 * (hlo - P.hmin), (hlo + 1.0 * P.hmin) * m))
-    return 1.0;
-  double f = dmax(0.0, dmin(P.c_tmp * dmax(hlo, 0.0) / hc_e + P.d_tmp,
-                            dmin(P.c_tmp * dmax(hc, 0.0) / hhi_e + P.d_tmp, 1.0)));
-  f = dmin(1.2 * dmax(hlo - P.hmin, 0.0) / (dmax(hlo, 0.0) + 1.0 * P.hmin), f);
+  const bool a1 = dgt0(hlo) && dge(hlo, 0.30000000000000004 * hc_e * m);
+  const bool b1 = dge(hc, 0.30000000000000004 * hhi_e * m);
+  const bool c1 = dgt0(hlo) && dge(1.2 * (hlo - P.hmin), (hlo + 1.0 * P.hmin) * m);
+  if (a1 && b1 && c1) return 1.0;
+  // f = max(0, min(A, min(B, 1))), then min(C, f): a term proved >= 1 does
+  // not change either minimum, so it is not divided out
+  const double bt = b1 ? 1.0 : dmin(P.c_tmp * dmax(hc, 0.0) / hhi_e + P.d_tmp, 1.0);
+  const double at = a1 ? bt : dmin(P.c_tmp * dmax(hlo, 0.0) / hc_e + P.d_tmp, bt);
+  double f = dmax(0.0, at);
+  if (!c1) f = dmin(1.2 * dmax(hlo - P.hmin, 0.0) / (dmax(hlo, 0.0) + 1.0 * P.hmin), f);
   return f;
 }
 
@@ -308,11 +334,14 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
     const double hlo = dmin(dmin(h0, dmin(h1, h2)), hk);
     const double hhi = dmax(dmax(h0, dmax(h1, h2)), hk);
     const double hf = wet_dry_factor(P, hk, hlo, hhi);
-    double beta = P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hf;
-    reconstruct3(beta, w[k], w[s.x], w[s.y], w[s.z], G, E.w);
-    reconstruct3(beta, hk, h0, h1, h2, G, E.h);
-    const double beta_u = P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hf;
-    const double beta_v = P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hf;
+    // at hf == 1 the betas and their reciprocals are the precomputed ones
+    const bool one = dbits(hf) == dbits(1.0);
+    const double beta = one ? P.beta_w1 : P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hf;
+    const double ib = one ? P.inv_beta_w1 : 0.0;
+    reconstruct3(beta, ib, w[k], w[s.x], w[s.y], w[s.z], G, E.w);
+    reconstruct3(beta, ib, hk, h0, h1, h2, G, E.h);
+    const double beta_u = one ? P.beta_uh1 : P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hf;
+    const double beta_v = one ? P.beta_vh1 : P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hf;
     double u0 = u[s.x], u1 = u[s.y], u2 = u[s.z];
     double v0 = v[s.x], v1 = v[s.y], v2 = v[s.z];
     // Neighbour velocities can be stale-zeroed only for a dry cell k (a wet
@@ -330,19 +359,19 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
       if (s.y == k) { u1 = uk; v1 = vk; }
       if (s.z == k) { u2 = uk; v2 = vk; }
     }
-    reconstruct3(beta_u, uk, u0, u1, u2, G, E.uh);
-    reconstruct3(beta_v, vk, v0, v1, v2, G, E.vh);
+    reconstruct3(beta_u, one ? P.inv_beta_uh1 : 0.0, uk, u0, u1, u2, G, E.uh);
+    reconstruct3(beta_v, one ? P.inv_beta_vh1 : 0.0, vk, v0, v1, v2, G, E.vh);
   } else {
     int j = 0;
     const int sv[3] = {s.x, s.y, s.z};
     while (j < 2 && sv[j] == k) j++;
     const int kn = sv[j];
-    reconstruct_towards(P.beta_w, w[k], w[kn], G, E.w);
-    reconstruct_towards(P.beta_w, hk, h[kn], G, E.h);
+    reconstruct_towards(P.beta_w, P.inv_beta_w, w[k], w[kn], G, E.w);
+    reconstruct_towards(P.beta_w, P.inv_beta_w, hk, h[kn], G, E.h);
     double un, vn;
     neighbour_uv(P, kn, meta_before(meta, j) != 0, surr, h, u, v, un, vn);
-    reconstruct_towards(P.beta_w, uk, un, G, E.uh);
-    reconstruct_towards(P.beta_w, vk, vn, G, E.vh);
+    reconstruct_towards(P.beta_w, P.inv_beta_w, uk, un, G, E.uh);
+    reconstruct_towards(P.beta_w, P.inv_beta_w, vk, vn, G, E.vh);
   }
   if (P.velocity_extrapolation) {
     for (int i = 0; i < 3; i++) {
