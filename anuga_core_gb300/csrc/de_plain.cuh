@@ -201,6 +201,20 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
     pos[i] = kj > kpos;            // jump > tiny
   }
   const double ratio_floor = (!neg[0] && !pos[0]) ? 1.0 : 1000.0;
+  if (dbits(beta) == dbits(1.0)) {
+    // beta 1: fl(fl(r)*1) >= 1 exactly when r >= 1, i.e. hi >= d (d > 0) or
+    // lo <= d (d < 0); floor >= 1, so phi is 1 unless a ratio fails
+    bool fail[3], any = false;
+    for (int i = 0; i < 3; i++) {
+      fail[i] = neg[i] ? !dle(lo, jump[i]) : (pos[i] && !dge(hi, jump[i]));
+      any |= fail[i];
+    }
+    if (!any) return 1.0;
+    double r = ratio_floor;
+    for (int i = 0; i < 3; i++)
+      if (fail[i]) r = dmin((neg[i] ? lo : hi) / jump[i], r);
+    return dmin(r, 1.0);
+  }
   if (dgt0(beta)) {
     const double inv_beta = dgt0(inv_known) ? inv_known : 1.0 / beta;
     const double need = inv_beta * (1.0 + 9.094947017729282e-13);
@@ -232,6 +246,15 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
 //   nb==2 : g[6]=gradient factor x, g[7]=gradient factor y
 constexpr int GEO_STRIDE = 11;
 
+// Edge values qc + jump * phi (jump * 1 is jump: the product is skipped).
+AGX_HD void limited_edges(double qc, const double jump[3], double phi, double out[3]) {
+  if (dbits(phi) == dbits(1.0)) {
+    for (int i = 0; i < 3; i++) out[i] = qc + jump[i];
+  } else {
+    for (int i = 0; i < 3; i++) out[i] = qc + jump[i] * phi;
+  }
+}
+
 AGX_HD void reconstruct3(double beta, double inv_known, double qc, double q0, double q1, double q2,
                          const double* G, double out[3]) {
   if (!dgt0(beta)) {
@@ -250,7 +273,7 @@ AGX_HD void reconstruct3(double beta, double inv_known, double qc, double q0, do
   const double hi = dmax(dmax(d0, dmax(d0 + d1, d0 + d2)), 0.0);
   const double lo = dmin(dmin(d0, dmin(d0 + d1, d0 + d2)), 0.0);
   const double phi = limiter_phi(jump, lo, hi, beta, inv_known);
-  for (int i = 0; i < 3; i++) out[i] = qc + jump[i] * phi;
+  limited_edges(qc, jump, phi, out);
 }
 
 AGX_HD void reconstruct_towards(double beta, double inv_known, double qc, double qn, const double* G,
@@ -263,7 +286,7 @@ AGX_HD void reconstruct_towards(double beta, double inv_known, double qc, double
   double lo, hi;
   if (dge0(d)) { lo = 0.0; hi = d; } else { lo = d; hi = 0.0; }
   const double phi = limiter_phi(jump, lo, hi, beta, inv_known);
-  for (int i = 0; i < 3; i++) out[i] = qc + jump[i] * phi;
+  limited_edges(qc, jump, phi, out);
 }
 
 // Wet/dry blending factor (:1537-1551).  In deep water it is exactly 1 and
