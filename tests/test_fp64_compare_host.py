@@ -1,7 +1,12 @@
-"""The integer-pipe FP64 comparisons of the plain kernels (de_plain.cuh:
-dlt, dle, dgt, dge, dmax, dmin and the tests against zero) give the IEEE
-comparison's outcome for every non-NaN pair: checked on the host by
-tests/cpp/check_dcompare.cpp over special values and 2M random pairs."""
+"""Exactness of the plain kernels' restructured arithmetic, checked on the
+host from the same source (de_plain.cuh compiled by g++):
+
+* tests/cpp/check_dcompare.cpp: the integer-pipe FP64 comparisons (dlt, dle,
+  dgt, dge, dmax, dmin, the tests against zero) give the IEEE comparison's
+  outcome for every non-NaN pair (special values and 2M random pairs);
+* tests/cpp/check_limiter.cpp: the limiter (margin tests, failing ratios
+  only, one division per call) and the wet/dry factor equal the reference's
+  formulas bit for bit on 4M and 2M random and adversarial inputs."""
 import os
 import shutil
 import subprocess
@@ -11,13 +16,22 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def test_integer_comparisons_match_ieee(tmp_path):
+def _run(tmp_path, name):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("g++ not available")
-    exe = str(tmp_path / "check_dcompare")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-o", exe, os.path.join(HERE, "cpp", "check_dcompare.cpp")],
-                   check=True, capture_output=True, text=True)
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    exe = str(tmp_path / name)
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-o", exe,
+                    os.path.join(HERE, "cpp", name + ".cpp")], check=True, capture_output=True, text=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "mismatches 0" in r.stdout
+    return r.stdout
+
+
+def test_integer_comparisons_match_ieee(tmp_path):
+    assert "mismatches 0" in _run(tmp_path, "check_dcompare")
+
+
+def test_limiter_and_wet_dry_factor_match_reference_formulas(tmp_path):
+    out = _run(tmp_path, "check_limiter")
+    assert "mismatches 0" in out and "wet/dry mismatches 0" in out
