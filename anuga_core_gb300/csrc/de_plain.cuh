@@ -182,6 +182,27 @@ AGX_HD double prep_cell(const Params& P, int k, double* w, double* uh, double* v
 
 // ---- limited reconstruction ----------------------------------------------
 // __limit_gradient (:1195-1231).  `lo`/`hi` are the admissible jump range.
+// min(floor, fl(n_i / d_i)) over the failing slots i (n_i = lo where
+// d_i < 0, hi where d_i > 0).  The failing slots are gathered in order
+// first, second, third and divided in that order, so that the lanes of a
+// warp share one division for their first failing slot whichever slot it is.
+AGX_HD double min_failing_ratio(const bool fail[3], const bool neg[3], double lo, double hi,
+                                const double jump[3], double floor) {
+  const double n0 = neg[0] ? lo : hi, n1 = neg[1] ? lo : hi, n2 = neg[2] ? lo : hi;
+  // first failing slot, then the next ones
+  const double na = fail[0] ? n0 : (fail[1] ? n1 : n2);
+  const double da = fail[0] ? jump[0] : (fail[1] ? jump[1] : jump[2]);
+  const bool two = fail[0] ? (fail[1] || fail[2]) : (fail[1] && fail[2]);
+  const double nb = (fail[0] && fail[1]) ? n1 : n2;
+  const double db = (fail[0] && fail[1]) ? jump[1] : jump[2];
+  const bool three = fail[0] && fail[1] && fail[2];
+  if (!(fail[0] || fail[1] || fail[2])) return floor;
+  double r = dmin(na / da, floor);
+  if (two) r = dmin(nb / db, r);
+  if (three) r = dmin(n2 / jump[2], r);
+  return r;
+}
+
 // inv_known > 0 is 1/beta, formed beforehand; otherwise it is divided out.
 AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double beta, double inv_known) {
   const double tiny = 1.0e-100;
@@ -210,10 +231,7 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
       any |= fail[i];
     }
     if (!any) return 1.0;
-    double r = ratio_floor;
-    for (int i = 0; i < 3; i++)
-      if (fail[i]) r = dmin((neg[i] ? lo : hi) / jump[i], r);
-    return dmin(r, 1.0);
+    return dmin(min_failing_ratio(fail, neg, lo, hi, jump, ratio_floor), 1.0);
   }
   if (dgt0(beta)) {
     const double inv_beta = dgt0(inv_known) ? inv_known : 1.0 / beta;
@@ -225,10 +243,7 @@ AGX_HD double limiter_phi(const double jump[3], double lo, double hi, double bet
       any |= fail[i];
     }
     if (!any && dle(inv_beta, ratio_floor)) return dmin(ratio_floor * beta, 1.0);
-    double r = ratio_floor;
-    for (int i = 0; i < 3; i++)
-      if (fail[i]) r = dmin((neg[i] ? lo : hi) / jump[i], r);
-    return dmin(r * beta, 1.0);
+    return dmin(min_failing_ratio(fail, neg, lo, hi, jump, ratio_floor) * beta, 1.0);
   }
   double r = 1000.0, cand = 1.0;
   for (int i = 0; i < 3; i++) {
