@@ -24,6 +24,7 @@
 #include "agx_internal.cuh"
 #include "de_mixed.cuh"
 #include "inlet.cuh"
+#include "bits.cuh"
 #include "../../include/agx_pool.h"
 #include <algorithm>
 #include <cstdarg>
@@ -243,49 +244,6 @@ __device__ __forceinline__ float manning_x(const MParams& P, float h, float uh, 
   const float a = dt32 * S;
   if (!(a < 1.0e30f)) return 1.0f;
   return a / (1.0f + a);
-}
-
-// float <-> double conversions done with integer operations on the IEEE-754
-// bit layouts (sign, biased exponent, mantissa), so that they run on the
-// integer pipe instead of the FP64 pipe.  Normal numbers and zero convert
-// exactly (float -> double) or rounded to nearest (double -> float, ties away
-// from zero); values below the float normal range become signed zero.
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned int b = __float_as_uint(f);
-  const unsigned int e = (b >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
-  const unsigned long long mant = (unsigned long long)(b & 0x7fffffu) << 29;
-  const unsigned long long ex = (e == 255u) ? 2047ull : (unsigned long long)(e + 896u);
-  const unsigned long long r = (e == 0u) ? sign : (sign | (ex << 52) | mant);
-  return __longlong_as_double((long long)r);
-}
-
-__device__ __forceinline__ float d2f_bits(double x) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  b &= 0x7fffffffffffffffull;
-  b += (1ull << 28);
-  const int e = (int)(b >> 52) - 896;
-  if (e <= 0) return __uint_as_float(sign);
-  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
-  return __uint_as_float(sign | ((unsigned int)e << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
-}
-
-__device__ __forceinline__ bool negative_bits(double x) { return __double_as_longlong(x) < 0; }
-
-// 0.5 a + 0.5 b with one FP64 add: halving by decrementing the exponent is
-// exact for normal numbers, so the result is bitwise that of the product form
-// (which rounds once, after two exact halvings); zero, subnormal and
-// non-finite operands take the product form.
-__device__ __forceinline__ double half_sum(double a, double b) {
-  const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
-  const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);
-  const double s = a + b;
-  const long long bits = __double_as_longlong(s);
-  const int es = (int)((bits >> 52) & 0x7ff);
-  if (ea > 1 && eb > 1 && es > 1 && es < 0x7ff && ea < 0x7ff && eb < 0x7ff)
-    return __longlong_as_double(bits - (1ll << 52));
-  return 0.5 * a + 0.5 * b;
 }
 
 // Work record (depth, velocity) of a state whose depth w - z is `depth`

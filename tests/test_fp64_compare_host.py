@@ -6,7 +6,10 @@ host from the same source (de_plain.cuh compiled by g++):
   outcome for every non-NaN pair (special values and 2M random pairs);
 * tests/cpp/check_limiter.cpp: the limiter (margin tests, failing ratios
   only, one division per call) and the wet/dry factor equal the reference's
-  formulas bit for bit on 4M and 2M random and adversarial inputs."""
+  formulas bit for bit on 4M and 2M random and adversarial inputs;
+* tests/cpp/check_bits.cpp: the mixed update's integer-pipe conversions
+  (bits.cuh: f2d_bits, d2f_bits) and RK2 halving (half_sum) equal the
+  operations they replace."""
 import os
 import shutil
 import subprocess
@@ -35,3 +38,7 @@ def test_integer_comparisons_match_ieee(tmp_path):
 def test_limiter_and_wet_dry_factor_match_reference_formulas(tmp_path):
     out = _run(tmp_path, "check_limiter")
     assert "mismatches 0" in out and "wet/dry mismatches 0" in out
+
+
+def test_mixed_update_bit_conversions(tmp_path):
+    assert "mismatches 0" in _run(tmp_path, "check_bits")
