@@ -111,6 +111,7 @@ def load(path=None):
         "agx_update_conserved": ([H, ctypes.c_double, P(ctypes.c_int64)], ctypes.c_int32),
         "agx_backup": ([H], ctypes.c_int32),
         "agx_saxpy": ([H, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
+        "agx_divide_conserved": ([H, ctypes.c_double], ctypes.c_int32),
         "agx_set_clock": ([H, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
         "agx_advance": ([H, ctypes.c_int64, P(StepStats)], ctypes.c_int32),
         "agx_get_stats": ([H, P(StepStats)], ctypes.c_int32),
@@ -315,6 +316,9 @@ class Scenario:
 
     def saxpy(self, a, b):
         check(self.L.agx_saxpy(self.h, float(a), float(b)))
+
+    def divide(self, divisor):
+        check(self.L.agx_divide_conserved(self.h, float(divisor)))
 
     def set_clock(self, time, yield_time, final_time):
         check(self.L.agx_set_clock(self.h, float(time), float(yield_time), float(final_time)))

@@ -243,8 +243,8 @@ agx_status agx_scenario_create(const agx_mesh_desc* m, const agx_params* p, agx_
   *out = nullptr;
   if (m->n_cells < 0 || m->n_cells >= (1ll << 29) || m->n_boundary < 0 || m->n_edges < 0)
     return fail(AGX_E_INVALID, "mesh sizes out of range");
-  if (p->timestepping_method != 1 && p->timestepping_method != 2)
-    return fail(AGX_E_INVALID, "timestepping_method must be 1 (euler) or 2 (rk2)");
+  if (p->timestepping_method < 1 || p->timestepping_method > 3)
+    return fail(AGX_E_INVALID, "timestepping_method must be 1 (euler), 2 (rk2) or 3 (rk3)");
   if (p->precision != AGX_PREC_FP64)
     return fail(AGX_E_INVALID, "this entry point builds the plain FP64 form; use agx_mixed_create for mixed precision");
   agx_scenario* s = new agx_scenario();
@@ -585,6 +585,12 @@ agx_status agx_backup(agx_handle h) {
 agx_status agx_saxpy(agx_handle h, double a, double b) {
   if (!h) return fail(AGX_E_INVALID, "null handle");
   CK(enqueue_saxpy(h, h->stream, a, b));
+  return sync(h);
+}
+
+agx_status agx_divide_conserved(agx_handle h, double divisor) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  CK(enqueue_divide(h, h->stream, divisor));
   return sync(h);
 }
 

@@ -200,6 +200,7 @@ cudaError_t enqueue_update(Scenario* s, cudaStream_t st, int stage, bool use_clo
 cudaError_t enqueue_forcing(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_backup(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_saxpy(Scenario* s, cudaStream_t st, double a, double b);
+cudaError_t enqueue_divide(Scenario* s, cudaStream_t st, double divisor);
 cudaError_t enqueue_reset_accum(Scenario* s, cudaStream_t st);
 
 }  // namespace agx

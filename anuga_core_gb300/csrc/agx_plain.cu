@@ -8,6 +8,7 @@
 // One timestep is a fixed sequence of kernels (DE1 = RK2 shown):
 //   prep(backup) -> extrap -> bc -> flux -> accum(dt) -> timestep -> update
 //   -> prep -> extrap -> bc -> flux -> accum -> update(saxpy) -> rates -> clock
+// (DE2 = RK3 adds a third stage: generic_domain.py:2053-2172).
 // All state stays in device memory; the clock kernel decides on the device
 // whether another step is needed and sets the graph's while condition.
 #include "agx_internal.cuh"
@@ -141,7 +142,9 @@ __device__ void series_value(const double* rows, int n, double t, double out[3])
   for (int q = 0; q < 3; q++) out[q] = a[1 + q] + ratio * (c[1 + q] - a[1 + q]);
 }
 
-__global__ void k_bc(Dev d, double t_override, int stage2) {
+// Boundary values; a time series is read at t_override, or (NaN) at the
+// clock's time + frac * timestep (the stage's time: frac 0, 1 or 0.5).
+__global__ void k_bc(Dev d, double t_override, double frac) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= d.B) return;
   const int kind = d.bkind[m];
@@ -152,7 +155,7 @@ __global__ void k_bc(Dev d, double t_override, int stage2) {
   const double* val = d.bval + 3 * (size_t)m;
   if (kind == BK_TIME_SERIES) {
     double t = t_override;
-    if (t != t) t = d.clock->time + (stage2 ? d.clock->timestep : 0.0);  // NaN: use the clock
+    if (t != t) t = d.clock->time + frac * d.clock->timestep;  // NaN: use the clock
     series_value(d.bseries, d.nseries, t, tv);
     val = tv;
   }
@@ -242,6 +245,8 @@ __global__ void k_timestep(Dev d, int substep_count) {
   timestep_logic(d.clock);
 }
 
+// saxpy: 0 none; 1 RK2 combine 0.5 Q + 0.5 Q0; 2 RK3 second stage
+// 0.25 Q + 0.75 Q0; 3 RK3 last stage (2 Q + Q0) / 3 (generic_domain.py:2126, 2160-2166).
 __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int saxpy) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   int bad = 0, neg = 0;
@@ -267,9 +272,16 @@ __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int 
       vh = 0.0;
     }
     if (saxpy) {
-      w = 0.5 * w + 0.5 * d.w0[k];
-      uh = 0.5 * uh + 0.5 * d.uh0[k];
-      vh = 0.5 * vh + 0.5 * d.vh0[k];
+      const double a = saxpy == 2 ? 0.25 : (saxpy == 3 ? 2.0 : 0.5);
+      const double b = saxpy == 2 ? 0.75 : (saxpy == 3 ? 1.0 : 0.5);
+      w = a * w + b * d.w0[k];
+      uh = a * uh + b * d.uh0[k];
+      vh = a * vh + b * d.vh0[k];
+      if (saxpy == 3) {
+        w = w / 3.0;
+        uh = uh / 3.0;
+        vh = vh / 3.0;
+      }
     }
     d.w[k] = w;
     d.uh[k] = uh;
@@ -304,6 +316,16 @@ __global__ void k_backup(Dev d) {
   d.w0[k] = d.w[k];
   d.uh0[k] = d.uh[k];
   d.vh0[k] = d.vh[k];
+}
+
+// Conserved centroid values divided by `divisor` (the last RK3 stage's
+// Q / 3.0, generic_domain.py:2163-2166).
+__global__ void k_divide(Dev d, double divisor) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.N) return;
+  d.w[k] = d.w[k] / divisor;
+  d.uh[k] = d.uh[k] / divisor;
+  d.vh[k] = d.vh[k] / divisor;
 }
 
 __global__ void k_saxpy(Dev d, double a, double b) {
@@ -463,7 +485,7 @@ cudaError_t enqueue_protect(Scenario* s, cudaStream_t st) {
 cudaError_t enqueue_boundary(Scenario* s, cudaStream_t st, double t_override, bool stage2) {
   const Dev& d = s->d;
   if (d.B == 0) return cudaSuccess;
-  LAUNCHK(PH_BC, k_bc<<<nblk(d.B), TPB, 0, st>>>(d, t_override, stage2 ? 1 : 0));
+  LAUNCHK(PH_BC, k_bc<<<nblk(d.B), TPB, 0, st>>>(d, t_override, stage2 ? 1.0 : 0.0));
   return cudaSuccess;
 }
 
@@ -498,21 +520,28 @@ cudaError_t enqueue_backup(Scenario* s, cudaStream_t st) {
   return cudaSuccess;
 }
 
+cudaError_t enqueue_divide(Scenario* s, cudaStream_t st, double divisor) {
+  if (s->d.N == 0) return cudaSuccess;
+  LAUNCH(k_divide<<<nblk(s->d.N), TPB, 0, st>>>(s->d, divisor));
+  return cudaSuccess;
+}
+
 cudaError_t enqueue_saxpy(Scenario* s, cudaStream_t st, double a, double b) {
   if (s->d.N == 0) return cudaSuccess;
   LAUNCH(k_saxpy<<<nblk(s->d.N), TPB, 0, st>>>(s->d, a, b));
   return cudaSuccess;
 }
 
-// One full timestep (Euler or RK2), ending with the clock kernel.
+// One full timestep (Euler, RK2 or RK3), ending with the clock kernel.
 cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_handle, bool set_cond) {
   const Dev& d = s->d;
   const int nb = nblk(d.N), eb = nblk(d.E), bb = nblk(d.B);
   const bool rk2 = s->prm.timestepping_method == 2;
+  const bool rk3 = s->prm.timestepping_method == 3;
   // stage 1
-  LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, rk2 ? 1 : 0));
+  LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, (rk2 || rk3) ? 1 : 0));
   LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
-  if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 0));
+  if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 0.0));
   LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
   LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
   LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 0));
@@ -521,12 +550,32 @@ cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_h
   if (rk2) {
     LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, 0));
     LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
-    if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 1));
+    if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 1.0));
     LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
     LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
     LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 1));
     LAUNCH(k_store_bfs<<<1, 1, 0, st>>>(d, 1));
     LAUNCHK(PH_UPDATE, k_update<<<nb, TPB, 0, st>>>(d, 2, 1, 0.0, 1));
+  }
+  if (rk3) {
+    // second stage at t + dt, combined to 0.25 Q + 0.75 Q0
+    LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, 0));
+    LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
+    if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 1.0));
+    LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
+    LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
+    LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 1));
+    LAUNCH(k_store_bfs<<<1, 1, 0, st>>>(d, 1));
+    LAUNCHK(PH_UPDATE, k_update<<<nb, TPB, 0, st>>>(d, 2, 1, 0.0, 2));
+    // third stage at t + dt/2, combined to (2 Q + Q0) / 3
+    LAUNCHK(PH_PREP, k_prep<<<nb, TPB, 0, st>>>(d, 0));
+    LAUNCHK(PH_EXTRAP, k_extrap<false><<<nb, TPB, 0, st>>>(d));
+    if (d.B) LAUNCHK(PH_BC, k_bc<<<bb, TPB, 0, st>>>(d, kNaN, 0.5));
+    LAUNCH(k_reset_accum<<<1, 1, 0, st>>>(d));
+    LAUNCHK(PH_FLUX, k_flux<<<eb, TPB, 0, st>>>(d));
+    LAUNCHK(PH_ACCUM, k_accum<<<nb, TPB, 0, st>>>(d, 2));
+    LAUNCH(k_store_bfs<<<1, 1, 0, st>>>(d, 2));
+    LAUNCHK(PH_UPDATE, k_update<<<nb, TPB, 0, st>>>(d, 3, 1, 0.0, 3));
   }
   for (size_t i = 0; i < s->ops.size(); i++) {
     const RateOp& op = s->ops[i];

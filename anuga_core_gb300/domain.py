@@ -34,12 +34,20 @@ MIN_TIMESTEP = 1.0e-6    # anuga/config.py min_timestep
 MAX_SMALLSTEPS = 50      # anuga/config.py max_smallsteps
 
 # shallow_water_domain.py:583-707
+# shallow_water/shallow_water_domain.py:583-877 (_set_DE*_defaults)
 FLOW_ALGORITHMS = {
     "DE0": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
                 beta_w=0.5, beta_w_dry=0.0, beta_uh=0.5, beta_uh_dry=0.0, beta_vh=0.5, beta_vh_dry=0.0),
     "DE1": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-5,
                 beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+    "DE2": dict(CFL=1.0, timestepping_method="rk3", minimum_allowed_height=1.0e-5,
+                beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+    "DE0_7": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
+                  beta_w=0.7, beta_w_dry=0.1, beta_uh=0.7, beta_uh_dry=0.1, beta_vh=0.7, beta_vh_dry=0.1),
+    "DE1_7": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-12,
+                  beta_w=0.75, beta_w_dry=0.1, beta_uh=0.75, beta_uh_dry=0.1, beta_vh=0.75, beta_vh_dry=0.1),
 }
+_TIMESTEPPING = {"euler": 1, "rk2": 2, "rk3": 3}
 
 _STATE_FIELDS = ("stage_c", "xmom_c", "ymom_c")     # pulled eagerly at every yield
 _SYNCED, _DEV_NEWER, _HOST_NEWER = 0, 1, 2
@@ -185,9 +193,9 @@ class Domain:
     # ------------------------------------------------------------------
     # configuration
     def set_flow_algorithm(self, flow_algorithm="DE0"):
-        flow_algorithm = str(flow_algorithm).upper()
+        flow_algorithm = str(flow_algorithm).upper().replace(".", "_")
         if flow_algorithm not in FLOW_ALGORITHMS:
-            raise ValueError("flow algorithm %s is not provided (DE0 and DE1 are)" % flow_algorithm)
+            raise ValueError("Unknown flow_algorithm. \nPossible choices are:\n" + ", ".join(FLOW_ALGORITHMS) + ".")
         d = FLOW_ALGORITHMS[flow_algorithm]
         self.flow_algorithm = flow_algorithm
         self.CFL = d["CFL"]
@@ -207,9 +215,9 @@ class Domain:
         self._invalidate_device()
 
     def set_timestepping_method(self, m):
-        m = {1: "euler", 2: "rk2"}.get(m, m)
-        if m not in ("euler", "rk2"):
-            raise ValueError("timestepping method %r not provided (euler, rk2)" % m)
+        m = {1: "euler", 2: "rk2", 3: "rk3"}.get(m, m)
+        if m not in _TIMESTEPPING:
+            raise ValueError("%s is an incorrect timestepping type" % (m,))
         self.timestepping_method = m
         self._invalidate_device()
 
@@ -366,7 +374,7 @@ class Domain:
         p.evolve_min_timestep = self.evolve_min_timestep
         p.extrapolate_velocity_second_order = 1 if self.extrapolate_velocity_second_order else 0
         p.low_froude = self.low_froude
-        p.timestepping_method = 1 if self.timestepping_method == "euler" else 2
+        p.timestepping_method = _TIMESTEPPING[self.timestepping_method]
         p.protect_zero_ymom = 1 if self.protect_zero_ymom else 0
         p.use_sloped_mannings = 1 if self.use_sloped_mannings else 0
         p.max_smallsteps = self.max_smallsteps
@@ -390,6 +398,8 @@ class Domain:
         if self.low_froude:
             per_side = np.ones((len(self), 3), bool)
         if self.precision == "mixed":
+            if self.timestepping_method == "rk3":
+                raise NotImplementedError("rk3 time stepping (DE2) runs on the plain FP64 form (precision='fp64')")
             from .mixed import MixedScenario
             self._scn = MixedScenario(self.mesh, None, self._params())
         else:
@@ -626,6 +636,40 @@ class Domain:
         self.update_conserved_quantities()
         self.saxpy_conserved_quantities(0.5, 0.5)
 
+    def evolve_one_rk3_step(self, yieldstep, finaltime):
+        """generic_domain.py:2053-2172: Q1 = E(dt) Q0; Q2 = 0.25 E(dt) Q1 + 0.75 Q0
+        (at t + dt/2); Q = (2 E(dt) Q2 + Q0) / 3."""
+        initial_time = self.get_relative_time()
+        self.backup_conserved_quantities()
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 0
+        self.compute_fluxes()
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+        self.set_relative_time(self.relative_time + self.timestep)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 1
+        self.compute_fluxes()
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy_conserved_quantities(0.25, 0.75)
+        self.set_relative_time(initial_time + self.timestep * 0.5)
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self._substep = 2
+        self.compute_fluxes()
+        self._substep = 0
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy_conserved_quantities(2.0, 1.0)
+        scn = self._ensure_device()
+        scn.divide(3.0)
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c"])
+        self.set_relative_time(initial_time + self.timestep)
+
     # ------------------------------------------------------------------
     # time stepping
     def _device_steps(self, max_steps=0):
@@ -687,6 +731,8 @@ class Domain:
         t0 = self.relative_time
         if self.timestepping_method == "euler":
             self.evolve_one_euler_step(yieldstep, finaltime)
+        elif self.timestepping_method == "rk3":
+            self.evolve_one_rk3_step(yieldstep, finaltime)
         else:
             self.evolve_one_rk2_step(yieldstep, finaltime)
         # operators: device ones through the library in one shot

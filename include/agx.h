@@ -64,7 +64,7 @@ typedef struct {
   double CFL, evolve_max_timestep, evolve_min_timestep;
   int32_t extrapolate_velocity_second_order;
   int32_t low_froude;
-  int32_t timestepping_method;   /* 1 = euler (DE0), 2 = rk2 (DE1) */
+  int32_t timestepping_method;   /* 1 = euler (DE0, DE0_7), 2 = rk2 (DE1, DE1_7), 3 = rk3 (DE2) */
   int32_t protect_zero_ymom;     /* 0: sw_domain_openmp.c:1139-1140 (xmom only); 1: orig (both) */
   int32_t use_sloped_mannings;
   int32_t max_smallsteps;
@@ -189,6 +189,9 @@ agx_status agx_update_conserved(agx_handle h, double timestep, int64_t* negative
  * (generic_domain.py:2187-2199). */
 agx_status agx_backup(agx_handle h);
 agx_status agx_saxpy(agx_handle h, double a, double b);
+/* Conserved centroid values divided by `divisor`: the last stage of
+ * evolve_one_rk3_step, Q.centroid_values / 3.0 (generic_domain.py:2160-2166). */
+agx_status agx_divide_conserved(agx_handle h, double divisor);
 
 /* ---- device step loop ------------------------------------------------------ */
 

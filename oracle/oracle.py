@@ -9,6 +9,7 @@ The loop mirrors the reference:
 * ``_evolve_base``            abstract_2d_finite_volumes/generic_domain.py:1715-1912
 * ``evolve_one_euler_step``   generic_domain.py:1914-1972
 * ``evolve_one_rk2_step``     generic_domain.py:1974-2051
+* ``evolve_one_rk3_step``     generic_domain.py:2053-2172
 * ``update_timestep``         generic_domain.py:2349-2415
 * ``update_conserved_quantities`` shallow_water/shallow_water_domain.py:2089-2163
 * ``Rate_operator.__call__``  operators/rate_operators.py:149-258 (constant rates)
@@ -117,17 +118,23 @@ def _p(a):
     return a.ctypes.data_as(_ip)
 
 
-# Algorithm defaults, shallow_water/shallow_water_domain.py:583-707
+# Algorithm defaults, shallow_water/shallow_water_domain.py:583-877
 FLOW_DEFAULTS = {
     "DE0": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
                 beta_w=0.5, beta_w_dry=0.0, beta_uh=0.5, beta_uh_dry=0.0, beta_vh=0.5, beta_vh_dry=0.0),
     "DE1": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-5,
                 beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+    "DE2": dict(CFL=1.0, timestepping_method="rk3", minimum_allowed_height=1.0e-5,
+                beta_w=1.0, beta_w_dry=0.0, beta_uh=1.0, beta_uh_dry=0.0, beta_vh=1.0, beta_vh_dry=0.0),
+    "DE0_7": dict(CFL=0.9, timestepping_method="euler", minimum_allowed_height=1.0e-12,
+                  beta_w=0.7, beta_w_dry=0.1, beta_uh=0.7, beta_uh_dry=0.1, beta_vh=0.7, beta_vh_dry=0.1),
+    "DE1_7": dict(CFL=1.0, timestepping_method="rk2", minimum_allowed_height=1.0e-12,
+                  beta_w=0.75, beta_w_dry=0.1, beta_uh=0.75, beta_uh_dry=0.1, beta_vh=0.75, beta_vh_dry=0.1),
 }
 
 
 class OracleDomain:
-    """A DE0/DE1 domain advanced by the CPU oracle.
+    """A DE-family domain (DE0, DE1, DE2, DE0_7, DE1_7) advanced by the CPU oracle.
 
     ``mesh`` is any object with the reference's mesh attributes (the
     product's ``anuga_core_gb300.mesh.Mesh`` or a reference ``Domain``).
@@ -145,7 +152,7 @@ class OracleDomain:
         self.flow_algorithm = flow_algorithm
         self.CFL = d["CFL"]
         self.timestepping_method = d["timestepping_method"]
-        self.timestep_fluxcalls = 1 if self.timestepping_method == "euler" else 2
+        self.timestep_fluxcalls = {"euler": 1, "rk2": 2, "rk3": 3}[self.timestepping_method]
         self.evolve_max_timestep = 1.0e3    # anuga/config.py max_timestep
         self.evolve_min_timestep = 1.0e-6   # anuga/config.py min_timestep
         self.max_smallsteps = 50
@@ -416,6 +423,34 @@ class OracleDomain:
         self.update_conserved_quantities()
         self.saxpy(0.5, 0.5)
 
+    def rk3_step(self, yieldstep, finaltime):
+        t0 = self.relative_time
+        self.backup()
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(0)
+        self.compute_forcing_terms()
+        self.update_timestep(yieldstep, finaltime)
+        self.update_conserved_quantities()
+        self.relative_time = self.relative_time + self.timestep
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(1)
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy(0.25, 0.75)
+        self.relative_time = t0 + self.timestep * 0.5
+        self.distribute_to_vertices_and_edges()
+        self.update_boundary()
+        self.compute_fluxes(2)
+        self.compute_forcing_terms()
+        self.update_conserved_quantities()
+        self.saxpy(2.0, 1.0)
+        for q in ("stage", "xmom", "ymom"):
+            c = getattr(self, q + "_c")
+            c[:] = c / 3.0
+        self.relative_time = t0 + self.timestep
+
     def evolve(self, yieldstep=None, finaltime=None, max_steps=None):
         """Generator with the reference's yield semantics; ``max_steps``
         stops after that many steps (the step-count form of the benchmark)."""
@@ -435,6 +470,8 @@ class OracleDomain:
             t0 = self.relative_time
             if self.timestepping_method == "euler":
                 self.euler_step(yieldstep, finaltime)
+            elif self.timestepping_method == "rk3":
+                self.rk3_step(yieldstep, finaltime)
             else:
                 self.rk2_step(yieldstep, finaltime)
             self.apply_fractional_steps()

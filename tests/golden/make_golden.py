@@ -222,8 +222,19 @@ def build_inlets(m=12, n=8):
     return d, extra
 
 
+def flow_algorithm_fixtures():
+    # the other flow algorithms of the DE family (shallow_water_domain.py:708-877):
+    # DE2 (rk3 time stepping), DE0_7 and DE1_7 (other betas, minimum height)
+    trajectory_fixture("traj_dambreak_de2.npz", build_dam_break, "DE2", 1.0, 3.0)
+    trajectory_fixture("traj_inflow_de2.npz", build_inflow_bumps, "DE2", 10.0, 30.0)
+    trajectory_fixture("traj_inflow_de0_7.npz", build_inflow_bumps, "DE0_7", 10.0, 30.0)
+    trajectory_fixture("traj_inflow_de1_7.npz", build_inflow_bumps, "DE1_7", 10.0, 30.0)
+
+
 if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "flows":
+    flow_algorithm_fixtures()
 elif __name__ == "__main__":
     p, e, b = anuga.rectangular_cross(3, 2, 3.0, 2.0)
     mesh_fixture("mesh_rect_3x2.npz", p, e, b)
@@ -235,3 +246,4 @@ elif __name__ == "__main__":
     trajectory_fixture("traj_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 40.0)
     trajectory_fixture("traj_delaunay_rain_de1.npz", build_delaunay_rain, "DE1", 2.0, 6.0)
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
+    flow_algorithm_fixtures()

@@ -43,6 +43,28 @@ def test_inflow_bumps_depth_error_within_1mm(oracle_mod):
     assert abs(d.total_steps - od.total_steps) <= max(2, od.total_steps // 50)
 
 
+@pytest.mark.parametrize("alg", ["DE0_7", "DE1_7"])
+def test_other_flow_algorithms_depth_error_within_1mm(oracle_mod, alg):
+    """DE0_7 and DE1_7 (other betas and minimum height) on the mixed form."""
+    d = workloads.inflow_bumps(m=40, L=400.0, flow_algorithm=alg, precision="mixed")
+    kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+             "top": ("reflective", None), "bottom": ("reflective", None)}
+    od, _ = _oracle_for(oracle_mod, d, alg, kinds)
+    for _ in d.evolve(yieldstep=10.0, finaltime=40.0):
+        pass
+    for _ in od.evolve(yieldstep=10.0, finaltime=40.0):
+        pass
+    z = d.quantities["elevation"].centroid_values
+    err = np.abs(np.maximum(d.quantities["stage"].centroid_values - z, 0) - np.maximum(od.stage_c - od.bed_c, 0)).max()
+    assert err <= DEPTH_TOL, err
+
+
+def test_rk3_is_refused_by_the_mixed_form():
+    d = workloads.dam_break(m=8, flow_algorithm="DE2", precision="mixed")
+    with pytest.raises(NotImplementedError, match="rk3"):
+        d._ensure_device()
+
+
 def test_dam_break_de0_depth_error_within_1mm(oracle_mod):
     d = workloads.dam_break(m=40, precision="mixed")
     kinds = {t: ("reflective", None) for t in ("left", "right", "top", "bottom")}

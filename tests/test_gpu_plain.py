@@ -68,6 +68,13 @@ TRAJ = {
     "traj_inflow_de1": ("DE1", {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
                                 "top": ("reflective", None), "bottom": ("reflective", None)}, False),
     "traj_delaunay_rain_de1": ("DE1", {"exterior": ("reflective", None)}, True),
+    "traj_dambreak_de2": ("DE2", {t: ("reflective", None) for t in ("left", "right", "top", "bottom")}, False),
+    "traj_inflow_de2": ("DE2", {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+                                "top": ("reflective", None), "bottom": ("reflective", None)}, False),
+    "traj_inflow_de0_7": ("DE0_7", {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+                                    "top": ("reflective", None), "bottom": ("reflective", None)}, False),
+    "traj_inflow_de1_7": ("DE1_7", {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+                                    "top": ("reflective", None), "bottom": ("reflective", None)}, False),
 }
 
 
@@ -309,6 +316,27 @@ def test_rate_given_as_a_function_runs_on_the_device():
     assert out[0][1] == out[1][1]
     assert np.array_equal(out[0][0], out[1][0])
     assert out[0][2] > 0 and abs(out[0][2] - out[1][2]) <= 1e-12 * out[0][2]
+
+
+def test_rk3_host_steps_equal_the_device_loop():
+    """DE2 (rk3) through the per-phase host step (a rate given as a function
+    of time) and through the device step loop (the same constant rate):
+    bitwise the same states and step counts."""
+    from anuga_core_gb300 import workloads
+    out = []
+    for rate in (1.0e-4, lambda t: 1.0e-4):
+        d = workloads.dam_break(m=16, flow_algorithm="DE2")
+        assert d.get_timestepping_method() == "rk3"
+        idx = np.arange(0, len(d), 2)
+        op = agx.Rate_operator(d, rate=rate, indices=idx)
+        for _ in d.evolve(yieldstep=0.5, finaltime=2.0):
+            pass
+        assert d._device_loop_ok() == (not callable(rate))
+        out.append((d.quantities["stage"].centroid_values.copy(), d.quantities["xmomentum"].centroid_values.copy(),
+                    d.total_steps, op.get_Q()))
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert abs(out[0][3] - out[1][3]) <= 1e-12 * abs(out[0][3])
 
 
 INLET_REGIONS = {"a": ([[10.0, 20.0], [30.0, 20.0], [30.0, 60.0], [10.0, 60.0]], {}),

@@ -55,6 +55,13 @@ TRAJ = {
     "traj_inflow_de1": ("DE1", {"left": ("dirichlet", (2.0, 0, 0)), "right": ("transmissive", None),
                                 "top": R, "bottom": R}, False),
     "traj_delaunay_rain_de1": ("DE1", {"exterior": R}, True),
+    "traj_dambreak_de2": ("DE2", {"left": R, "right": R, "top": R, "bottom": R}, False),
+    "traj_inflow_de2": ("DE2", {"left": ("dirichlet", (2.0, 0, 0)), "right": ("transmissive", None),
+                                "top": R, "bottom": R}, False),
+    "traj_inflow_de0_7": ("DE0_7", {"left": ("dirichlet", (2.0, 0, 0)), "right": ("transmissive", None),
+                                    "top": R, "bottom": R}, False),
+    "traj_inflow_de1_7": ("DE1_7", {"left": ("dirichlet", (2.0, 0, 0)), "right": ("transmissive", None),
+                                    "top": R, "bottom": R}, False),
 }
 
 
