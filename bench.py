@@ -356,7 +356,7 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
         fp = _lib.fp64_throughput()
         roof["fp64_measured"] = fp
         roof["note"] = ("FP64-pipe bound: the measured FP64 rates (fp64_measured, G ops/s) are 1/54 of the FP32 "
-                        "rate; ncu shows the extrapolation kernel's FP64 pipe 83%% busy at 6%% of HBM bandwidth "
+                        "rate; ncu shows the extrapolation kernel's FP64 pipe 84% busy at 6% of HBM bandwidth "
                         "(profiles/k_extrap_inflow_bumps_1M_fp64.md)")
     alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
     ach_s = alg_step / (ms_per_step / 1e3) / 1e9
@@ -399,10 +399,15 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # category's launches of one step, divided by the cells of the captured mesh).
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
-        "bytes_per_cell": (117.267712e6 + 11.5648e6 + 177.335808e6 + 25.904384e6) / 1.0e6,
+        "bytes_per_cell": (117.630976e6 + 11.483136e6 + 169.704960e6 + 24.624896e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
-                "(m=500, MINB=4 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
+                "(m=500, MINB=6 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
                 "scaled by cells; profiles/k_pool_flux_inflow_bumps_1M_mixed.md"},
+    ("fp64", "extrap"): {
+        "bytes_per_cell": 2 * (125.701632e6 + 78.489088e6) / 1.0e6,
+        "note": "ncu --set full of k_extrap<0> (edges only, flowing state) on the 1.0M-triangle inflow_bumps "
+                "case (m=500), dram__bytes_read.sum + dram__bytes_write.sum per launch x 2 launches per "
+                "DE1 step, scaled by cells; profiles/k_extrap_inflow_bumps_1M_fp64.md"},
 }
 
 
