@@ -112,6 +112,8 @@ def load(path=None):
         "agx_backup": ([H], ctypes.c_int32),
         "agx_saxpy": ([H, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
         "agx_divide_conserved": ([H, ctypes.c_double], ctypes.c_int32),
+        "agx_set_riverwalls": ([H, _i32p, ctypes.c_int64, ctypes.c_int64, _f64p, _i32p, ctypes.c_int32,
+                                ctypes.c_int32, _f64p], ctypes.c_int32),
         "agx_set_clock": ([H, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
         "agx_advance": ([H, ctypes.c_int64, P(StepStats)], ctypes.c_int32),
         "agx_get_stats": ([H, P(StepStats)], ctypes.c_int32),
@@ -319,6 +321,14 @@ class Scenario:
 
     def divide(self, divisor):
         check(self.L.agx_divide_conserved(self.h, float(divisor)))
+
+    def set_riverwalls(self, edge_counter, elevation, row_index, hydraulic):
+        cnt = np.ascontiguousarray(edge_counter, np.int32)
+        el = np.ascontiguousarray(elevation, np.float64)
+        row = np.ascontiguousarray(row_index, np.int32)
+        hyd = np.ascontiguousarray(hydraulic, np.float64)
+        check(self.L.agx_set_riverwalls(self.h, ptr_i32(cnt), cnt.size, el.size, el.ctypes.data_as(_f64p),
+                                        ptr_i32(row), hyd.shape[0], hyd.shape[1], hyd.ctypes.data_as(_f64p)))
 
     def set_clock(self, time, yield_time, final_time):
         check(self.L.agx_set_clock(self.h, float(time), float(yield_time), float(final_time)))

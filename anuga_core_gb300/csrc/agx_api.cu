@@ -327,6 +327,7 @@ agx_status agx_scenario_destroy(agx_handle h) {
   if (s->node_slot) cudaFree(s->node_slot);
   if (s->frame) cudaFree(s->frame);
   if (s->bseries) cudaFree(s->bseries);
+  if (s->rw_mem) cudaFree(s->rw_mem);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->own_stream) cudaStreamSynchronize(s->own_stream);
   if (s->arena) cudaFree(s->arena);
@@ -585,6 +586,52 @@ agx_status agx_backup(agx_handle h) {
 agx_status agx_saxpy(agx_handle h, double a, double b) {
   if (!h) return fail(AGX_E_INVALID, "null handle");
   CK(enqueue_saxpy(h, h->stream, a, b));
+  return sync(h);
+}
+
+agx_status agx_set_riverwalls(agx_handle h, const int32_t* edge_counter, int64_t n_slots, int64_t n_riverwall_edges,
+                              const double* elevation, const int32_t* row_index, int32_t n_rows, int32_t ncol,
+                              const double* hydraulic) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  if (n_slots != 3 * (int64_t)h->N) return fail(AGX_E_INVALID, "edge_counter has %lld slots, the mesh %lld",
+                                                (long long)n_slots, 3 * (long long)h->N);
+  if (n_riverwall_edges < 0 || (n_riverwall_edges > 0 && (!edge_counter || !elevation || !row_index || !hydraulic)) ||
+      n_rows <= 0 || ncol < 5)
+    return fail(AGX_E_INVALID, "bad riverwall tables (need 5 hydraulic columns: Qfactor s1 s2 h1 h2)");
+  for (int64_t s = 0; n_riverwall_edges > 0 && s < n_slots; s++)
+    if (edge_counter[s] < 0 || edge_counter[s] > n_riverwall_edges)
+      return fail(AGX_E_INVALID, "riverwall counter %d at slot %lld out of range", edge_counter[s], (long long)s);
+  for (int64_t r = 0; r < n_riverwall_edges; r++)
+    if (row_index[r] < 0 || row_index[r] >= n_rows)
+      return fail(AGX_E_INVALID, "riverwall row index %d out of range", row_index[r]);
+  agx_status st = sync(h);
+  if (st) return st;
+  if (h->rw_mem) cudaFree(h->rw_mem);
+  h->rw_mem = nullptr;
+  h->d.rw_counter = nullptr;
+  h->d.rw_elev = nullptr;
+  h->d.rw_row = nullptr;
+  h->d.rw_hyd = nullptr;
+  h->d.rw_ncol = 0;
+  h->graph_valid = false;
+  if (n_riverwall_edges == 0) return AGX_OK;
+  const size_t b_counter = ((size_t)n_slots * 4 + 255) & ~(size_t)255;
+  const size_t b_elev = ((size_t)n_riverwall_edges * 8 + 255) & ~(size_t)255;
+  const size_t b_row = ((size_t)n_riverwall_edges * 4 + 255) & ~(size_t)255;
+  const size_t b_hyd = (size_t)n_rows * ncol * 8;
+  char* m = nullptr;
+  CK(cudaMalloc((void**)&m, b_counter + b_elev + b_row + b_hyd));
+  h->rw_mem = m;
+  CK(cudaMemcpyAsync(m, edge_counter, (size_t)n_slots * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(m + b_counter, elevation, (size_t)n_riverwall_edges * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(m + b_counter + b_elev, row_index, (size_t)n_riverwall_edges * 4, cudaMemcpyHostToDevice,
+                     h->stream));
+  CK(cudaMemcpyAsync(m + b_counter + b_elev + b_row, hydraulic, b_hyd, cudaMemcpyHostToDevice, h->stream));
+  h->d.rw_counter = (const int*)m;
+  h->d.rw_elev = (const double*)(m + b_counter);
+  h->d.rw_row = (const int*)(m + b_counter + b_elev);
+  h->d.rw_hyd = (const double*)(m + b_counter + b_elev + b_row);
+  h->d.rw_ncol = ncol;
   return sync(h);
 }
 

@@ -145,6 +145,14 @@ struct Dev {
   double *max_speed;
   double *sl0, *sl1, *sl2, *slsp, *slpf, *slhl;
   Clock* clock;
+  // riverwalls (structures/riverwall.py): per slot the 1-based riverwall
+  // edge (0: ordinary edge), crest elevation and hydraulic-table row per
+  // riverwall edge, the table [rows][rw_ncol]; all null without riverwalls
+  const int* rw_counter;
+  const double* rw_elev;
+  const int* rw_row;
+  const double* rw_hyd;
+  int rw_ncol;
 };
 
 struct Scenario {
@@ -174,6 +182,7 @@ struct Scenario {
   cudaGraphExec_t exec = nullptr;
   bool graph_valid = false;
   int kernels_per_step = 0;
+  void* rw_mem = nullptr;                // riverwall tables (one allocation)
 };
 
 // launch accounting

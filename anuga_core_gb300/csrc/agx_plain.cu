@@ -172,7 +172,7 @@ __global__ void k_flux(Dev d) {
   if (e >= d.E) return;
   const int s = d.edge_slot[e];
   const int k = s / 3, i = s - 3 * k;
-  const Riverwall RW = {nullptr, nullptr, nullptr, nullptr, 0};
+  const Riverwall RW = {d.rw_counter, d.rw_elev, d.rw_row, d.rw_hyd, d.rw_ncol};
   SlotResult R;
   double hr;
   slot_flux(d.P, k, i, d.conn[k], d.we, d.uhe, d.vhe, d.ze, d.he, d.wb, d.uhb, d.vhb, d.normals, d.w,

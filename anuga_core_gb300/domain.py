@@ -122,6 +122,13 @@ class Domain:
         self.writer = None
         self.minimum_storable_height = 1.0e-3
         self.set_flow_algorithm("DE0")
+        # riverwalls (structures/riverwall.py; shallow_water_domain.py:366-379)
+        self.edge_flux_type = np.zeros(3 * len(mesh), np.int64)
+        self.edge_river_wall_counter = np.zeros(3 * len(mesh), np.int64)
+        self.number_of_riverwall_edges = 0
+        from .riverwall import RiverWall
+        self.riverwallData = RiverWall(self)
+        self.create_riverwalls = self.riverwallData.create_riverwalls
         self.quantities["x"].set_values(self.mesh.vertex_coordinates[:, 0].reshape(-1, 3))
         self.quantities["y"].set_values(self.mesh.vertex_coordinates[:, 1].reshape(-1, 3))
         self._mass_added_seen = 0.0
@@ -390,6 +397,9 @@ class Domain:
             for f in self._fstate:
                 self._fstate[f] = _SYNCED
 
+    def _riverwalls_changed(self):
+        self._invalidate_device()
+
     def _ensure_device(self):
         if self._scn is not None:
             return self._scn
@@ -397,16 +407,27 @@ class Domain:
         per_side = None
         if self.low_froude:
             per_side = np.ones((len(self), 3), bool)
+        rw = self.riverwallData
+        if rw.active:
+            # the weir correction uses each side's own heads: no shared edge flux
+            marks = (self.edge_flux_type == 1).reshape(-1, 3)
+            per_side = marks if per_side is None else (per_side | marks)
         if self.precision == "mixed":
             if self.timestepping_method == "rk3":
                 raise NotImplementedError("rk3 time stepping (DE2) runs on the plain FP64 form (precision='fp64')")
+            if rw.active:
+                raise NotImplementedError("riverwalls run on the plain FP64 form (precision='fp64')")
             from .mixed import MixedScenario
             self._scn = MixedScenario(self.mesh, None, self._params())
         else:
-            if not hasattr(self, "_tables") or self._tables_key != (self.low_froude,):
+            key = (self.low_froude, tuple(rw.riverwall_edges) if rw.active else ())
+            if not hasattr(self, "_tables") or self._tables_key != key:
                 self._tables = pack_tables(self.mesh, per_side_edges=per_side)
-                self._tables_key = (self.low_froude,)
+                self._tables_key = key
             self._scn = _lib.Scenario(self._tables, self._params())
+            if rw.active:
+                self._scn.set_riverwalls(self.edge_river_wall_counter, rw.riverwall_elevation,
+                                         rw.hydraulic_properties_rowIndex, rw.hydraulic_properties)
         up = self._upload_fields()
         for f in self._fstate:
             if f in up:

@@ -189,6 +189,17 @@ agx_status agx_update_conserved(agx_handle h, double timestep, int64_t* negative
  * (generic_domain.py:2187-2199). */
 agx_status agx_backup(agx_handle h);
 agx_status agx_saxpy(agx_handle h, double a, double b);
+/* Riverwalls (structures/riverwall.py create_riverwalls; the weir branch of
+ * the flux, sw_domain_openmp.c:324-426, 581-650): edge_counter[n_slots = 3N]
+ * is the reference's edge_river_wall_counter (1-based riverwall edge of each
+ * slot, 0 for ordinary edges); elevation and row_index[n_riverwall_edges] the
+ * crest elevation and hydraulic-table row of each riverwall edge;
+ * hydraulic[n_rows * ncol] the table (columns Qfactor, s1, s2, h1, h2).  The
+ * mesh tables must evaluate riverwall slots per side (agx_mesh_desc edge
+ * list: no shared edge flux for them).  n_riverwall_edges = 0 removes them. */
+agx_status agx_set_riverwalls(agx_handle h, const int32_t* edge_counter, int64_t n_slots, int64_t n_riverwall_edges,
+                              const double* elevation, const int32_t* row_index, int32_t n_rows, int32_t ncol,
+                              const double* hydraulic);
 /* Conserved centroid values divided by `divisor`: the last stage of
  * evolve_one_rk3_step, Q.centroid_values / 3.0 (generic_domain.py:2160-2166). */
 agx_status agx_divide_conserved(agx_handle h, double divisor);

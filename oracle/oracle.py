@@ -238,6 +238,21 @@ class OracleDomain:
     def set_bed_vertex_values(self, zv):
         self.bed_v[:] = np.asarray(zv, np.float64).ravel()
 
+    def set_riverwalls(self, edge_flux_type, edge_river_wall_counter, riverwall_elevation,
+                       hydraulic_properties_rowIndex, hydraulic_properties):
+        """Riverwall tables in the reference's layout (structures/riverwall.py)."""
+        c = lambda a, t=np.float64: np.ascontiguousarray(a, dtype=t).ravel()
+        self.rw = dict(flux_type=c(edge_flux_type, np.int64), counter=c(edge_river_wall_counter, np.int64),
+                       row=c(hydraulic_properties_rowIndex, np.int64), elevation=c(riverwall_elevation),
+                       hyd=c(hydraulic_properties))
+        D = self.D
+        D.edge_flux_type = self.rw["flux_type"].ctypes.data_as(_ip)
+        D.edge_river_wall_counter = self.rw["counter"].ctypes.data_as(_ip)
+        D.riverwall_rowIndex = self.rw["row"].ctypes.data_as(_ip)
+        D.riverwall_elevation = _p(self.rw["elevation"])
+        D.riverwall_hydraulic_properties = _p(self.rw["hyd"])
+        D.ncol_riverwall_hydraulic_properties = np.asarray(hydraulic_properties).shape[-1]
+
     def set_boundaries(self, boundaries):
         self.boundaries = [(np.ascontiguousarray(ids, np.int64), kind, vals)
                            for ids, kind, vals in boundaries]

@@ -222,6 +222,27 @@ def build_inlets(m=12, n=8):
     return d, extra
 
 
+RIVERWALLS = {"south": [[50.0, 0.0, -2.2], [50.0, 50.0, -2.0]],
+              "north": [[50.0, 50.0, -2.0], [50.0, 80.0, -1.7], [50.0, 100.0, -1.9]]}
+RIVERWALL_PAR = {"north": {"Qfactor": 0.8, "s1": 0.85}}
+
+
+def build_dam_break_riverwall(m=20):
+    # the dam break with a levee on the dam line, overtopped along part of it
+    d, extra = build_dam_break(m)
+    d.set_flow_algorithm("DE1")
+    d.riverwallData.create_riverwalls(RIVERWALLS, RIVERWALL_PAR, verbose=False)
+    rw = d.riverwallData
+    extra = dict(extra)
+    extra["rw.edge_flux_type"] = np.asarray(d.edge_flux_type).copy()
+    extra["rw.edge_river_wall_counter"] = np.asarray(d.edge_river_wall_counter).copy()
+    extra["rw.riverwall_elevation"] = np.asarray(rw.riverwall_elevation).copy()
+    extra["rw.hydraulic_properties_rowIndex"] = np.asarray(rw.hydraulic_properties_rowIndex).copy()
+    extra["rw.hydraulic_properties"] = np.asarray(rw.hydraulic_properties).copy()
+    extra["rw.riverwall_edges"] = np.asarray(rw.riverwall_edges).copy()
+    return d, extra
+
+
 def flow_algorithm_fixtures():
     # the other flow algorithms of the DE family (shallow_water_domain.py:708-877):
     # DE2 (rk3 time stepping), DE0_7 and DE1_7 (other betas, minimum height)
@@ -235,6 +256,8 @@ if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "flows":
     flow_algorithm_fixtures()
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "riverwall":
+    trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)
 elif __name__ == "__main__":
     p, e, b = anuga.rectangular_cross(3, 2, 3.0, 2.0)
     mesh_fixture("mesh_rect_3x2.npz", p, e, b)
@@ -247,3 +270,4 @@ elif __name__ == "__main__":
     trajectory_fixture("traj_delaunay_rain_de1.npz", build_delaunay_rain, "DE1", 2.0, 6.0)
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
     flow_algorithm_fixtures()
+    trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)

@@ -318,6 +318,47 @@ def test_rate_given_as_a_function_runs_on_the_device():
     assert out[0][2] > 0 and abs(out[0][2] - out[1][2]) <= 1e-12 * out[0][2]
 
 
+RIVERWALLS = {"south": [[50.0, 0.0, -2.2], [50.0, 50.0, -2.0]],
+              "north": [[50.0, 50.0, -2.0], [50.0, 80.0, -1.7], [50.0, 100.0, -1.9]]}
+
+
+def test_riverwall_trajectory_matches_reference(golden):
+    """Two riverwalls on the dam line (weir flux, per-side evaluation of the
+    wall edges) against the reference's trajectory."""
+    f = golden("traj_riverwall_de1.npz")
+    m = int(f["mesh.m"])
+    p, e, b = rectangular_cross(m, m, 100.0, 100.0)
+    state = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"],
+                 elevation=f["init.elevation_c"], friction=f["init.friction"])
+    d = make_domain(p, e, b, "DE1", state, {t: ("reflective", None) for t in ("left", "right", "top", "bottom")})
+    d.create_riverwalls(RIVERWALLS, {"north": {"Qfactor": 0.8, "s1": 0.85}})
+    assert np.array_equal(d.edge_river_wall_counter, f["rw.edge_river_wall_counter"])
+    steps = []
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        steps.append(d.number_of_steps)
+        Q = d.quantities
+        assert normwise(Q["stage"].centroid_values, f["stage"][i]) <= STATE_TOL, i
+        assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
+        assert normwise(Q["ymomentum"].centroid_values, f["ymom"][i]) <= 1e-10, i
+    assert steps == list(f["steps"])
+    # the walls hold part of the water back: the run differs from one without them
+    d2 = make_domain(p, e, b, "DE1", state, {t: ("reflective", None) for t in ("left", "right", "top", "bottom")})
+    for _ in d2.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"])):
+        pass
+    assert np.abs(d2.quantities["stage"].centroid_values - f["stage"][-1]).max() > 1e-3
+
+
+def test_riverwalls_are_refused_by_the_mixed_form(golden):
+    f = golden("traj_riverwall_de1.npz")
+    p, e, b = rectangular_cross(int(f["mesh.m"]), int(f["mesh.m"]), 100.0, 100.0)
+    d = agx.Domain(p, e, b)
+    d.set_flow_algorithm("DE1")
+    d.set_gpu_options(precision="mixed")
+    d.create_riverwalls(RIVERWALLS)
+    with pytest.raises(NotImplementedError, match="riverwall"):
+        d._ensure_device()
+
+
 def test_rk3_host_steps_equal_the_device_loop():
     """DE2 (rk3) through the per-phase host step (a rate given as a function
     of time) and through the device step loop (the same constant rate):

@@ -118,3 +118,26 @@ def test_oracle_inlets_bit_exact(golden, oracle_mod):
         assert np.array_equal(r[2], f["stage"][i]), i
         assert np.array_equal(r[3], f["xmom"][i]), i
         assert np.array_equal(r[4], f["ymom"][i]), i
+
+
+def test_oracle_riverwall_trajectory_bit_exact(golden, oracle_mod):
+    """The weir branch of the flux (sw_domain_openmp.c:324-426, 581-650) on a
+    dam break whose dam line carries two riverwalls, against the reference."""
+    f = golden("traj_riverwall_de1.npz")
+    m = int(f["mesh.m"])
+    p, e, b = rectangular_cross(m, m, 100.0, 100.0)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, "DE1")
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    od.set_boundaries([(M.tag_boundary_cells[t], "reflective", None) for t in M.tag_boundary_cells])
+    od.set_riverwalls(f["rw.edge_flux_type"], f["rw.edge_river_wall_counter"], f["rw.riverwall_elevation"],
+                      f["rw.hydraulic_properties_rowIndex"], f["rw.hydraulic_properties"])
+    res = [(t, od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy(), od.ymom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["times"])
+    assert [r[1] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[2], f["stage"][i]), i
+        assert np.array_equal(r[3], f["xmom"][i]), i
+        assert np.array_equal(r[4], f["ymom"][i]), i
