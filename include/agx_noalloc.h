@@ -65,6 +65,7 @@ typedef struct {
  * together) race on it and give wrong results; serialise them.  The first call
  * on each device looks up the scratch address (cudaGetSymbolAddress, which
  * may load the module); make that first call before any stream capture.
+ * Riverwalls are not applied: every edge takes the plain central flux.
  * err (may be NULL) receives a message of at most err_len bytes on failure. */
 agx_status agx_compute_fluxes_noalloc(const agx_params* params, const agx_flux_buffers* buf, int32_t substep,
                                       void* stream, double* flux_timestep, double* boundary_flux_sum,
