@@ -75,6 +75,11 @@ struct PoolDev {
   const int* bkind;
   const double* bval;
   const int* bcell;
+  // riverwalls (only read where conn.w bit 20 + i marks slot i a wall edge):
+  // crest elevation and hydraulic-table row per slot, the table [row][5]
+  const double* rw_crest;
+  const int* rw_row;
+  const float* rw_hyd;
 };
 
 __device__ __forceinline__ int nb_of(int meta) { return (meta >> 16) & 3; }
@@ -328,7 +333,7 @@ __device__ float block_sum_f(float x, float* sh) {
 // cells (the outside neighbours its edges need) into shared memory; phase 2
 // evaluates the three edge fluxes of every own cell from shared memory and
 // accumulates them.  FUSED2: stage 2 of RK2 (update and combine fused in).
-template <bool FUSED2, int MINB>
+template <bool FUSED2, int MINB, bool RW = false>
 __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
   __shared__ float shf[TILE / 32];
@@ -469,7 +474,23 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
           }
         }
         Flux32 F;
-        central_flux32(L.h, L.uh, L.vh, hre, uhr, vhr, dd, n1, n2, P, F);
+        if (RW && ((cn.w >> (20 + i)) & 1)) {
+          // riverwall edge (sw_domain_openmp.c:581-650), all heights relative
+          // to this edge's bed zl: crest c, Audusse bed zh = max(0, zr - zl, c)
+          const size_t q = 3 * (size_t)k + i;
+          const float c = (float)(d.rw_crest[q] - d.z[k]) - L.dz;
+          central_flux32<true>(L.h, L.uh, L.vh, hre, uhr, vhr, dd, n1, n2, P, F, c);
+          const float zh = fmaxf(fmaxf(dd, 0.0f), c);
+          // neighbour centroid bed - zl; on a boundary edge the reference
+          // takes the cell's own centroid and zr = zl for the far head
+          const float zn = n >= 0 ? dzn[i] - L.dz : -L.dz;
+          const float hl_c = fmaxf(rk.x - L.dz - zh, 0.0f);      // own centroid stage - z_half
+          const float hr_c = n >= 0 ? fmaxf(W[n].x + zn - zh, 0.0f) : fmaxf(rk.x + dd - zh, 0.0f);
+          const float weir_height = fmaxf(c - fminf(dd, 0.0f), 0.0f);
+          if (c > fmaxf(-L.dz, zn)) weir_adjust32(F, hl_c, hr_c, P.g, weir_height, d.rw_hyd + 5 * d.rw_row[q]);
+        } else {
+          central_flux32(L.h, L.uh, L.vh, hre, uhr, vhr, dd, n1, n2, P, F);
+        }
         const float e0 = -F.f0 * len;
         const float e1 = -F.f1 * len;
         const float e2 = -F.f2 * len;
@@ -868,6 +889,10 @@ struct Pool {
   size_t snap_bytes = 0;
   int kernels_per_iter = 0;
   int mode_rk2_any = 1;
+  bool rw_any = false;           // some scenario has riverwalls: the flux kernels take the wall branch
+  void* rw_mem = nullptr;        // per-slot riverwall crest and row (3 x cap_cells)
+  float* rw_hyd_dev = nullptr;   // hydraulic table, rows of 5
+  std::vector<float> rw_hyd;     // host copy of the table
 };
 
 static thread_local char g_perr[512] = "";
@@ -990,7 +1015,8 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->variant == 0) k_pool_flux<false, 6><<<Gf, TILE, 0, st>>>(d);
+  if (p->rw_any) k_pool_flux<false, 6, true><<<Gf, TILE, 0, st>>>(d);
+  else if (p->variant == 0) k_pool_flux<false, 6><<<Gf, TILE, 0, st>>>(d);
   else k_pool_flux<false, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
@@ -1010,7 +1036,8 @@ static cudaError_t enqueue_second_stage(Pool* p, cudaStream_t st, unsigned long 
   const PoolDev& d = p->d;
   const int S = p->cap_scn;
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->variant == 0) k_pool_flux<true, 6><<<Gf, TILE, 0, st>>>(d);
+  if (p->rw_any) k_pool_flux<true, 6, true><<<Gf, TILE, 0, st>>>(d);
+  else if (p->variant == 0) k_pool_flux<true, 6><<<Gf, TILE, 0, st>>>(d);
   else k_pool_flux<true, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
@@ -1144,6 +1171,8 @@ agx_status agx_pool_destroy(agx_pool p) {
   }
   if (p->arena) cudaFree(p->arena);
   if (p->snap) cudaFree(p->snap);
+  if (p->rw_mem) cudaFree(p->rw_mem);
+  if (p->rw_hyd_dev) cudaFree(p->rw_hyd_dev);
   if (p->scn_host) cudaFreeHost(p->scn_host);
   if (p->own_stream) cudaStreamDestroy(p->own_stream);
   delete p;
@@ -1650,6 +1679,90 @@ agx_status agx_pool_add_inlet(agx_pool p, int32_t sid, const int32_t* idx, int64
   op.vv = velocity_v;
   op.area = area;
   return pool_add_op(p, sid, idx, n, op);
+}
+
+// Sets (or, with n_riverwall_edges = 0, removes) the wall bits 20 + i of
+// the scenario's conn meta words.
+__global__ void k_pool_rw_bits(int4* conn, const int* bits, int n) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int4 c = conn[j];
+  c.w = (c.w & ~(7 << 20)) | (bits[j] << 20);
+  conn[j] = c;
+}
+
+agx_status agx_pool_set_riverwalls(agx_pool p, int32_t sid, const int32_t* edge_counter, int64_t n_slots,
+                                   int64_t n_riverwall_edges, const double* elevation, const int32_t* row_index,
+                                   int32_t n_rows, int32_t ncol, const double* hydraulic) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (n_slots != 3 * (int64_t)sh.N) return pfail(AGX_E_INVALID, "edge_counter has %lld slots, the mesh %lld",
+                                                 (long long)n_slots, 3 * (long long)sh.N);
+  if (n_riverwall_edges < 0 || (n_riverwall_edges > 0 && (!edge_counter || !elevation || !row_index || !hydraulic)) ||
+      (n_riverwall_edges > 0 && (n_rows <= 0 || ncol < 5)))
+    return pfail(AGX_E_INVALID, "bad riverwall tables (need 5 hydraulic columns: Qfactor s1 s2 h1 h2)");
+  for (int64_t s = 0; n_riverwall_edges > 0 && s < n_slots; s++)
+    if (edge_counter[s] < 0 || edge_counter[s] > n_riverwall_edges)
+      return pfail(AGX_E_INVALID, "riverwall counter %d at slot %lld out of range", edge_counter[s], (long long)s);
+  for (int64_t r = 0; r < n_riverwall_edges; r++)
+    if (row_index[r] < 0 || row_index[r] >= n_rows) return pfail(AGX_E_INVALID, "riverwall row index out of range");
+  agx_status st = psync(p);
+  if (st) return st;
+  const size_t C3 = 3 * (size_t)p->cap_cells;
+  const size_t b_crest = (C3 * 8 + 255) & ~(size_t)255;
+  if (!p->rw_mem && n_riverwall_edges > 0) {
+    PCK(cudaMalloc(&p->rw_mem, b_crest + C3 * 4));
+    PCK(cudaMemsetAsync(p->rw_mem, 0, b_crest + C3 * 4, p->stream));
+    p->d.rw_crest = (const double*)p->rw_mem;
+    p->d.rw_row = (const int*)((char*)p->rw_mem + b_crest);
+  }
+  // hydraulic rows of this call appended to the pool's table
+  const int row0 = (int)(p->rw_hyd.size() / 5);
+  for (int r = 0; r < n_rows && n_riverwall_edges > 0; r++)
+    for (int c = 0; c < 5; c++) p->rw_hyd.push_back((float)hydraulic[(size_t)r * ncol + c]);
+  if (n_riverwall_edges > 0) {
+    if (p->rw_hyd_dev) cudaFree(p->rw_hyd_dev);
+    p->rw_hyd_dev = nullptr;
+    PCK(cudaMalloc(&p->rw_hyd_dev, p->rw_hyd.size() * 4));
+    PCK(cudaMemcpyAsync(p->rw_hyd_dev, p->rw_hyd.data(), p->rw_hyd.size() * 4, cudaMemcpyHostToDevice, p->stream));
+    p->d.rw_hyd = p->rw_hyd_dev;
+  }
+  // per stored cell: wall bits, crest and row of each wall slot
+  std::vector<int32_t> ord(sh.N);
+  PCK(cudaMemcpyAsync(ord.data(), sh.order, sh.N * 4, cudaMemcpyDeviceToHost, p->stream));
+  if ((st = psync(p))) return st;
+  std::vector<int> bits(sh.N, 0);
+  std::vector<double> crest(3 * (size_t)sh.N, 0.0);
+  std::vector<int32_t> row(3 * (size_t)sh.N, 0);
+  bool any = false;
+  for (int j = 0; j < sh.N && n_riverwall_edges > 0; j++)
+    for (int i = 0; i < 3; i++) {
+      const int r = edge_counter[3 * (size_t)ord[j] + i];
+      if (r <= 0) continue;
+      bits[j] |= 1 << i;
+      crest[3 * (size_t)j + i] = elevation[r - 1];
+      row[3 * (size_t)j + i] = row0 + row_index[r - 1];
+      any = true;
+    }
+  const int c0 = sh.tile0 * TILE;
+  int* bits_dev = nullptr;
+  PCK(cudaMalloc(&bits_dev, sh.N * 4));
+  PCK(cudaMemcpyAsync(bits_dev, bits.data(), sh.N * 4, cudaMemcpyHostToDevice, p->stream));
+  k_pool_rw_bits<<<nblk1(sh.N), 256, 0, p->stream>>>((int4*)p->d.conn + c0, bits_dev, sh.N);
+  count_launch();
+  PCK(cudaGetLastError());
+  if (p->rw_mem) {
+    PCK(cudaMemcpyAsync((void*)(p->d.rw_crest + 3 * (size_t)c0), crest.data(), crest.size() * 8,
+                        cudaMemcpyHostToDevice, p->stream));
+    PCK(cudaMemcpyAsync((void*)(p->d.rw_row + 3 * (size_t)c0), row.data(), row.size() * 4, cudaMemcpyHostToDevice,
+                        p->stream));
+  }
+  st = psync(p);
+  cudaFree(bits_dev);
+  if (st) return st;
+  if (any) p->rw_any = true;
+  p->graph_valid = false;
+  return AGX_OK;
 }
 
 agx_status agx_pool_operators_from_host(agx_pool p, int32_t sid, int32_t on) {

@@ -76,17 +76,19 @@ __device__ __forceinline__ float wet_dry_factor32(const MParams& P, float hc, fl
 
 // Central-upwind flux across one edge (KNP), relative form.  Inputs: left
 // and right edge depths (unclamped) and momenta in the x/y frame, d = zr - zl,
-// normal (n1, n2).  Outputs the flux in the x/y frame, max speed, pressure
-// flux and the left/right Audusse depths.
+// normal (n1, n2); WALL: c = riverwall crest - zl raises the Audusse bed
+// z_half to max(zl, zr, crest) (sw_domain_openmp.c:581-588).  Outputs the flux
+// in the x/y frame, max speed, pressure flux and the left/right Audusse depths.
 struct Flux32 {
   float f0, f1, f2, speed, pflux, hl, hr;
 };
 
+template <bool WALL = false>
 __device__ __forceinline__ void central_flux32(float hle, float uhl_x, float vhl_x, float hre, float uhr_x,
                                                float vhr_x, float d, float n1, float n2, const MParams& P,
-                                               Flux32& F) {
-  const float hl = fmaxf(hle - fmaxf(d, 0.0f), 0.0f);
-  const float hr = fmaxf(hre - fmaxf(-d, 0.0f), 0.0f);
+                                               Flux32& F, float c = 0.0f) {
+  const float hl = WALL ? fmaxf(hle - fmaxf(fmaxf(d, 0.0f), c), 0.0f) : fmaxf(hle - fmaxf(d, 0.0f), 0.0f);
+  const float hr = WALL ? fmaxf(hre - fmaxf(fmaxf(-d, 0.0f), c - d), 0.0f) : fmaxf(hre - fmaxf(-d, 0.0f), 0.0f);
   F.hl = hl;
   F.hr = hr;
   if (hl == 0.0f && hr == 0.0f) {
@@ -154,6 +156,37 @@ __device__ __forceinline__ void central_flux32(float hle, float uhl_x, float vhl
   F.f0 = f0;
   F.f1 = n1 * f1 - n2 * f2;
   F.f2 = n2 * f1 + n1 * f2;
+}
+
+// Villemonte weir correction of a riverwall edge's flux (FP32 form of
+// __adjust_edgeflux_with_weir, sw_domain_openmp.c:324-426): hl, hr are the
+// first-order heads of the two centroids above z_half, hp = Qfactor, s1, s2,
+// h1, h2.
+__device__ __forceinline__ void weir_adjust32(Flux32& F, float hl, float hr, float g, float weir_height,
+                                              const float* hp) {
+  const float Qfactor = hp[0], s1 = hp[1], s2 = hp[2], h1 = hp[3], h2 = hp[4];
+  const float twothirds = 2.0f / 3.0f;
+  if ((hl <= 0.0f) && (hr <= 0.0f)) return;
+  const float minhd = fminf(hl, hr);
+  const float maxhd = fmaxf(hl, hr);
+  float rw = Qfactor * twothirds * maxhd * sqrtf(twothirds * g * maxhd);
+  const float rw2 = Qfactor * twothirds * minhd * sqrtf(twothirds * g * minhd);
+  const float rwRat = rw2 / fmaxf(rw, 1.0e-30f);
+  const float hdRat = minhd / fmaxf(maxhd, 1.0e-30f);
+  const float hdWrRat = minhd / fmaxf(weir_height, 1.0e-30f);
+  rw = rw * powf(1.0f - rwRat, 0.385f);
+  if (hr > hl) rw = -rw;
+  if ((hdRat < s2) & (hdWrRat < h2)) {
+    const float w1 = fminf(fmaxf(hdRat - s1, 0.0f) / (s2 - s1), 1.0f);
+    const float w2 = fminf(fmaxf(hdWrRat - h1, 0.0f) / (h2 - h1), 1.0f);
+    const float nf = (rw * (1.0f - w1) + w1 * F.f0) * (1.0f - w2) + w2 * F.f0;
+    float sc = (fabsf(F.f0) > 1.0e-30f) ? nf / F.f0 : 0.0f;
+    sc = fmaxf(sc, 0.0f);
+    F.f0 = nf;
+    F.f1 *= fminf(sc, 10.0f);
+    F.f2 *= fminf(sc, 10.0f);
+  }
+  if (fabsf(F.f0) > 0.0f) F.speed = sqrtf(g * (maxhd + weir_height)) + fabsf(F.f0 / (maxhd + 1.0e-12f));
 }
 
 }  // namespace agx

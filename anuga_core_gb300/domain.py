@@ -415,10 +415,11 @@ class Domain:
         if self.precision == "mixed":
             if self.timestepping_method == "rk3":
                 raise NotImplementedError("rk3 time stepping (DE2) runs on the plain FP64 form (precision='fp64')")
-            if rw.active:
-                raise NotImplementedError("riverwalls run on the plain FP64 form (precision='fp64')")
             from .mixed import MixedScenario
             self._scn = MixedScenario(self.mesh, None, self._params())
+            if rw.active:
+                self._scn.set_riverwalls(self.edge_river_wall_counter, rw.riverwall_elevation,
+                                         rw.hydraulic_properties_rowIndex, rw.hydraulic_properties)
         else:
             key = (self.low_froude, tuple(rw.riverwall_edges) if rw.active else ())
             if not hasattr(self, "_tables") or self._tables_key != key:

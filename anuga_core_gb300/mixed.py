@@ -50,6 +50,8 @@ def lib():
             "agx_pool_operators_from_host": ([H, ctypes.c_int32, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_apply_operator": ([H, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double], ctypes.c_int32),
+            "agx_pool_set_riverwalls": ([H, ctypes.c_int32, _i32p, ctypes.c_int64, ctypes.c_int64, _f64p, _i32p,
+                                         ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
             "agx_pool_clear_operators": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_set_clock": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -198,6 +200,15 @@ class Pool:
     def apply_operator(self, sid, op, rate, factor, timestep):
         check(self.L.agx_pool_apply_operator(self.h, sid, int(op), float(rate), float(factor), float(timestep)))
 
+    def set_riverwalls(self, sid, edge_counter, elevation, row_index, hydraulic):
+        cnt = np.ascontiguousarray(edge_counter, np.int32)
+        el = np.ascontiguousarray(elevation, np.float64)
+        row = np.ascontiguousarray(row_index, np.int32)
+        hyd = np.ascontiguousarray(hydraulic, np.float64).reshape(-1, 5)
+        check(self.L.agx_pool_set_riverwalls(self.h, sid, cnt.ctypes.data_as(_i32p), cnt.size, el.size,
+                                             el.ctypes.data_as(_f64p), row.ctypes.data_as(_i32p), hyd.shape[0],
+                                             hyd.shape[1], hyd.ctypes.data_as(_f64p)))
+
     def clear_operators(self, sid):
         check(self.L.agx_pool_clear_operators(self.h, sid))
 
@@ -344,6 +355,9 @@ class MixedScenario:
 
     def operators_from_host(self, on=True):
         self.pool.operators_from_host(self.sid, on)
+
+    def set_riverwalls(self, edge_counter, elevation, row_index, hydraulic):
+        self.pool.set_riverwalls(self.sid, edge_counter, elevation, row_index, hydraulic)
 
     def apply_operator(self, op, rate, factor, timestep):
         self.pool.apply_operator(self.sid, op, rate, factor, timestep)

@@ -82,6 +82,12 @@ agx_status agx_pool_operators_from_host(agx_pool p, int32_t sid, int32_t on);
  * agx_apply_operator. */
 agx_status agx_pool_apply_operator(agx_pool p, int32_t sid, int32_t op, double rate, double factor,
                                    double timestep);
+/* Riverwalls of one scenario, with the arguments of agx_set_riverwalls
+ * (edge_counter in the caller's cell order, 3 slots per cell); the pool's
+ * flux kernels take the weir branch on the marked slots (FP32). */
+agx_status agx_pool_set_riverwalls(agx_pool p, int32_t sid, const int32_t* edge_counter, int64_t n_slots,
+                                   int64_t n_riverwall_edges, const double* elevation, const int32_t* row_index,
+                                   int32_t n_rows, int32_t ncol, const double* hydraulic);
 agx_status agx_pool_clear_operators(agx_pool p, int32_t sid);
 agx_status agx_pool_operator_influx(agx_pool p, int32_t sid, int32_t op, double* influx);
 /* distribute_to_vertices_and_edges (shallow_water_domain.py:1879-1915). */

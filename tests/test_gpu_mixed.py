@@ -59,6 +59,27 @@ def test_other_flow_algorithms_depth_error_within_1mm(oracle_mod, alg):
     assert err <= DEPTH_TOL, err
 
 
+def test_riverwall_depth_error_within_1mm(golden):
+    """Two riverwalls on the dam line (FP32 weir branch of the pool's flux
+    kernels) against the reference's trajectory."""
+    from anuga_core_gb300.mesh import rectangular_cross as rc
+    f = golden("traj_riverwall_de1.npz")
+    m = int(f["mesh.m"])
+    p, e, b = rc(m, m, 100.0, 100.0)
+    state = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"],
+                 elevation=f["init.elevation_c"], friction=f["init.friction"])
+    walls = {"south": [[50.0, 0.0, -2.2], [50.0, 50.0, -2.0]],
+             "north": [[50.0, 50.0, -2.0], [50.0, 80.0, -1.7], [50.0, 100.0, -1.9]]}
+    d = make_domain(p, e, b, "DE1", state, {t: ("reflective", None) for t in ("left", "right", "top", "bottom")},
+                    precision="mixed")
+    d.create_riverwalls(walls, {"north": {"Qfactor": 0.8, "s1": 0.85}})
+    z = f["init.elevation_c"]
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        h = np.maximum(d.quantities["stage"].centroid_values - z, 0.0)
+        h_ref = np.maximum(f["stage"][i] - z, 0.0)
+        assert np.abs(h - h_ref).max() <= DEPTH_TOL, (i, np.abs(h - h_ref).max())
+
+
 def test_rk3_is_refused_by_the_mixed_form():
     d = workloads.dam_break(m=8, flow_algorithm="DE2", precision="mixed")
     with pytest.raises(NotImplementedError, match="rk3"):

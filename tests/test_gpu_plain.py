@@ -348,17 +348,6 @@ def test_riverwall_trajectory_matches_reference(golden):
     assert np.abs(d2.quantities["stage"].centroid_values - f["stage"][-1]).max() > 1e-3
 
 
-def test_riverwalls_are_refused_by_the_mixed_form(golden):
-    f = golden("traj_riverwall_de1.npz")
-    p, e, b = rectangular_cross(int(f["mesh.m"]), int(f["mesh.m"]), 100.0, 100.0)
-    d = agx.Domain(p, e, b)
-    d.set_flow_algorithm("DE1")
-    d.set_gpu_options(precision="mixed")
-    d.create_riverwalls(RIVERWALLS)
-    with pytest.raises(NotImplementedError, match="riverwall"):
-        d._ensure_device()
-
-
 def test_rk3_host_steps_equal_the_device_loop():
     """DE2 (rk3) through the per-phase host step (a rate given as a function
     of time) and through the device step loop (the same constant rate):
