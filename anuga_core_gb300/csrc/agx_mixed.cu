@@ -70,6 +70,7 @@ struct PoolDev {
   const double* area;
   float* eta;
   float4 *W0, *W1;           // work records (h, u, v, -) of stage 1 / stage 2
+  float4* W2;                // of the third RK3 stage (allocated with the first rk3 scenario)
   float4* E;                 // explicit update (ew, euh, evh, flags)
   float* maxs;
   const int* bkind;
@@ -332,13 +333,17 @@ __device__ float block_sum_f(float x, float* sh) {
 // Fused flux kernel.  Phase 1 reconstructs the tile's own cells and its halo
 // cells (the outside neighbours its edges need) into shared memory; phase 2
 // evaluates the three edge fluxes of every own cell from shared memory and
-// accumulates them.  FUSED2: stage 2 of RK2 (update and combine fused in).
-template <bool FUSED2, int MINB, bool RW = false>
+// accumulates them.  STG 1: first stage (explicit update and CFL minimum);
+// STG 2: second stage with the update and the combine fused in (RK2:
+// 0.5 Q + 0.5 Q0 into A; RK3: 0.25 Q + 0.75 Q0 into B); STG 3: third RK3
+// stage, (2 Q + Q0) / 3 into A (generic_domain.py:1974-2172).
+template <int STG, int MINB, bool RW = false>
 __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
+  constexpr bool FUSED2 = STG >= 2;
   __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
   __shared__ float shf[TILE / 32];
   __shared__ double shd[TILE / 32];
-  const float4* W = FUSED2 ? d.W1 : d.W0;
+  const float4* W = STG == 1 ? d.W0 : (STG == 2 ? d.W1 : d.W2);
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
     const int base = tile * TILE;
     const int k = base + threadIdx.x;
@@ -352,6 +357,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
     PoolScn* S = d.scn + sid;
     if (!S->active) continue;
     if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
+    if (STG == 3 && !S->P.rk3) continue;      // RK2 scenarios have two
     const MParams P = S->P;
     const bool valid = k < S->cell0 + S->ncell;
     bool sdry = false;
@@ -458,7 +464,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
             }
             case BK_TIME_SERIES: {
               double v3[3];
-              const double tnow = S->clock.time + (FUSED2 ? S->clock.timestep : 0.0);
+              const double tnow = S->clock.time + (STG == 1 ? 0.0 : (STG == 2 ? 1.0 : 0.5)) * S->clock.timestep;
               series_at(S->series, S->nseries, tnow, v3);
               hre = fmaxf((float)(v3[0] - d.z[k]) - L.dz, 0.0f);
               uhr = (float)v3[1];
@@ -528,20 +534,38 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         double h = sw, uh = suh, vh = svh;
         neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
                           S->clock.timestep32, added);
-        h = half_sum(h, d.wA[k]);
-        uh = half_sum(uh, d.uhA[k]);
-        vh = half_sum(vh, d.vhA[k]);
-        d.wA[k] = h;
-        d.uhA[k] = uh;
-        d.vhA[k] = vh;
-        d.W0[k] = record_of(P, h, uh, vh);     // work record of the next step
+        if (STG == 2 && !P.rk3) {
+          h = half_sum(h, d.wA[k]);
+          uh = half_sum(uh, d.uhA[k]);
+          vh = half_sum(vh, d.vhA[k]);
+          d.wA[k] = h;
+          d.uhA[k] = uh;
+          d.vhA[k] = vh;
+          d.W0[k] = record_of(P, h, uh, vh);     // work record of the next step
+        } else if (STG == 2) {                    // RK3: Q2 = 0.25 Q + 0.75 Q0 (depth-linear)
+          h = 0.25 * h + 0.75 * d.wA[k];
+          uh = 0.25 * uh + 0.75 * d.uhA[k];
+          vh = 0.25 * vh + 0.75 * d.vhA[k];
+          d.wB[k] = h;
+          d.uhB[k] = uh;
+          d.vhB[k] = vh;
+          d.W2[k] = record_of(P, h, uh, vh);     // work record of the third stage
+        } else {                                  // RK3: Q = (2 Q + Q0) / 3
+          h = (2.0 * h + d.wA[k]) / 3.0;
+          uh = (2.0 * uh + d.uhA[k]) / 3.0;
+          vh = (2.0 * vh + d.vhA[k]) / 3.0;
+          d.wA[k] = h;
+          d.uhA[k] = uh;
+          d.vhA[k] = vh;
+          d.W0[k] = record_of(P, h, uh, vh);
+        }
       }
       const float bs = block_sum_f(bfl, shf);
       const int anym = __syncthreads_or(__double_as_longlong(added) != 0);
       const double ma = anym ? block_sum_d(added, shd) : 0.0;
       const int nneg = __syncthreads_count(neg);
       if (threadIdx.x == 0) {
-        if (bs != 0.0f) atomicAdd(&S->clock.bfs[1], (double)bs);
+        if (bs != 0.0f) atomicAdd(&S->clock.bfs[STG == 3 ? 2 : 1], (double)bs);
         if (ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
         if (nneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)nneg);
       }
@@ -890,6 +914,9 @@ struct Pool {
   int kernels_per_iter = 0;
   int mode_rk2_any = 1;
   bool rw_any = false;           // some scenario has riverwalls: the flux kernels take the wall branch
+  bool rk3_any = false;          // some scenario has three stages: the third-stage flux kernel runs
+  int stages_done = 0;           // stages run by agx_pool_step_begin / _stage in the current split step
+  void* w2_mem = nullptr;        // third-stage work records
   void* rw_mem = nullptr;        // per-slot riverwall crest and row (3 x cap_cells)
   float* rw_hyd_dev = nullptr;   // hydraulic table, rows of 5
   std::vector<float> rw_hyd;     // host copy of the table
@@ -983,9 +1010,9 @@ static MParams make_mparams(const agx_params& a) {
   P.c_tmp = (float)c;
   P.d_tmp = (float)(1.0 - c * 0.3);
   P.velocity_extrapolation = a.extrapolate_velocity_second_order == 1;
-  P.rk2 = a.timestepping_method == 2;
+  P.rk2 = a.timestepping_method >= 2;
   P.low_froude = a.low_froude;
-  P.pad = 0;
+  P.rk3 = a.timestepping_method == 3;
   return P;
 }
 
@@ -1015,9 +1042,9 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->rw_any) k_pool_flux<false, 6, true><<<Gf, TILE, 0, st>>>(d);
-  else if (p->variant == 0) k_pool_flux<false, 6><<<Gf, TILE, 0, st>>>(d);
-  else k_pool_flux<false, 8><<<Gf, TILE, 0, st>>>(d);
+  if (p->rw_any) k_pool_flux<1, 6, true><<<Gf, TILE, 0, st>>>(d);
+  else if (p->variant == 0) k_pool_flux<1, 6><<<Gf, TILE, 0, st>>>(d);
+  else k_pool_flux<1, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
   k_pool_timestep<<<nblk1(S), 256, 0, st>>>(d, S);
@@ -1032,15 +1059,29 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-static cudaError_t enqueue_second_stage(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+// Flux kernel of stage 2 or 3 (stage 3 only when some scenario has three).
+static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
   const PoolDev& d = p->d;
-  const int S = p->cap_scn;
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->rw_any) k_pool_flux<true, 6, true><<<Gf, TILE, 0, st>>>(d);
-  else if (p->variant == 0) k_pool_flux<true, 6><<<Gf, TILE, 0, st>>>(d);
-  else k_pool_flux<true, 8><<<Gf, TILE, 0, st>>>(d);
+  if (stage == 3 && !p->rk3_any) return cudaSuccess;
+  if (stage == 2) {
+    if (p->rw_any) k_pool_flux<2, 6, true><<<Gf, TILE, 0, st>>>(d);
+    else if (p->variant == 0) k_pool_flux<2, 6><<<Gf, TILE, 0, st>>>(d);
+    else k_pool_flux<2, 8><<<Gf, TILE, 0, st>>>(d);
+  } else {
+    if (p->rw_any) k_pool_flux<3, 6, true><<<Gf, TILE, 0, st>>>(d);
+    else if (p->variant == 0) k_pool_flux<3, 6><<<Gf, TILE, 0, st>>>(d);
+    else k_pool_flux<3, 8><<<Gf, TILE, 0, st>>>(d);
+  }
   count_launch();
   phase_mark(st, PH_FLUX);
+  return cudaGetLastError();
+}
+
+// The operators of the step loop and the clocks.
+static cudaError_t enqueue_step_end(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  const PoolDev& d = p->d;
+  const int S = p->cap_scn;
   for (size_t s = 0; s < p->scn.size(); s++) {
     const ScnHost& sh = p->scn[s];
     if (!sh.alive || sh.host_ops) continue;
@@ -1060,8 +1101,10 @@ static cudaError_t enqueue_second_stage(Pool* p, cudaStream_t st, unsigned long 
 
 static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
   cudaError_t e = enqueue_first_stage(p, st);
+  if (e == cudaSuccess) e = enqueue_later_stage(p, st, 2);
+  if (e == cudaSuccess) e = enqueue_later_stage(p, st, 3);
   if (e != cudaSuccess) return e;
-  return enqueue_second_stage(p, st, h, set_cond);
+  return enqueue_step_end(p, st, h, set_cond);
 }
 
 static agx_status pool_build_graph(Pool* p) {
@@ -1134,8 +1177,8 @@ agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
   if (st) return st;
   int sms = 0, per = 0, per4 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<false, 6>, TILE, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pool_flux<false, 8>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_flux<1, 6>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per4, k_pool_flux<1, 8>, TILE, 0);
   p->grid = std::max(1, sms * std::max(per, 1));
   p->grid_v[0] = p->grid;
   p->grid_v[1] = std::max(1, sms * std::max(per4, 1));
@@ -1172,6 +1215,7 @@ agx_status agx_pool_destroy(agx_pool p) {
   if (p->arena) cudaFree(p->arena);
   if (p->snap) cudaFree(p->snap);
   if (p->rw_mem) cudaFree(p->rw_mem);
+  if (p->w2_mem) cudaFree(p->w2_mem);
   if (p->rw_hyd_dev) cudaFree(p->rw_hyd_dev);
   if (p->scn_host) cudaFreeHost(p->scn_host);
   if (p->own_stream) cudaStreamDestroy(p->own_stream);
@@ -1200,11 +1244,19 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
   if (!p || !conn || !geo || !area || !order || !prm || !sid_out || !lnk || !halo_off || !halo_cnt || N <= 0 ||
       B < 0 || n_halo < 0)
     return pfail(AGX_E_INVALID, "bad arguments");
-  if (prm->timestepping_method != 1 && prm->timestepping_method != 2)
-    return pfail(AGX_E_INVALID, "timestepping_method must be 1 or 2");
+  if (prm->timestepping_method < 1 || prm->timestepping_method > 3)
+    return pfail(AGX_E_INVALID, "timestepping_method must be 1, 2 or 3");
   int sid = -1;
   for (int s = 0; s < p->cap_scn; s++) if (!p->scn[s].alive) { sid = s; break; }
   if (sid < 0) return pfail(AGX_E_NOMEM, "pool has no free scenario slot");
+  if (prm->timestepping_method == 3 && !p->w2_mem) {      // third-stage work records
+    PCK(cudaMalloc(&p->w2_mem, (size_t)p->cap_cells * 16));
+    p->d.W2 = (float4*)p->w2_mem;
+  }
+  if (prm->timestepping_method == 3) {
+    p->rk3_any = true;
+    p->graph_valid = false;
+  }
   const int nt = (int)((N + TILE - 1) / TILE);
   int t0 = -1;
   for (int t = 0, run = 0; t < p->cap_tiles; t++) {
@@ -1894,12 +1946,25 @@ agx_status agx_pool_step_begin(agx_pool p) {
   for (int s = 0; s < p->cap_scn; s++)
     if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
   PCK(enqueue_first_stage(p, p->stream));
+  p->stages_done = 1;
+  return psync(p);
+}
+
+agx_status agx_pool_step_stage(agx_pool p, int32_t stage) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  if (stage != p->stages_done + 1 || stage < 2 || stage > 3)
+    return pfail(AGX_E_STATE, "stage %d out of order (stage %d ran last)", stage, p->stages_done);
+  PCK(enqueue_later_stage(p, p->stream, stage));
+  p->stages_done = stage;
   return psync(p);
 }
 
 agx_status agx_pool_step_end(agx_pool p, int32_t* n_done) {
   if (!p) return pfail(AGX_E_INVALID, "null pool");
-  PCK(enqueue_second_stage(p, p->stream, 0ull, false));
+  if (p->stages_done < 1) return pfail(AGX_E_STATE, "agx_pool_step_begin has not run");
+  for (int stage = p->stages_done + 1; stage <= 3; stage++) PCK(enqueue_later_stage(p, p->stream, stage));
+  p->stages_done = 0;
+  PCK(enqueue_step_end(p, p->stream, 0ull, false));
   agx_status st = pull_scn(p);
   if (st) return st;
   int done = 0;

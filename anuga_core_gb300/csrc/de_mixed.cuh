@@ -28,9 +28,9 @@ struct MParams {            // per-scenario parameters
   float c_tmp, d_tmp;
   double hmin64;
   int velocity_extrapolation;
-  int rk2;
+  int rk2;                  // two or more stages (rk2 or rk3)
   int low_froude;
-  int pad;
+  int rk3;                  // three stages (rk3, DE2)
 };
 
 struct EdgeState {          // one edge of one cell, relative to that cell

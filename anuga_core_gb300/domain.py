@@ -413,8 +413,6 @@ class Domain:
             marks = (self.edge_flux_type == 1).reshape(-1, 3)
             per_side = marks if per_side is None else (per_side | marks)
         if self.precision == "mixed":
-            if self.timestepping_method == "rk3":
-                raise NotImplementedError("rk3 time stepping (DE2) runs on the plain FP64 form (precision='fp64')")
             from .mixed import MixedScenario
             self._scn = MixedScenario(self.mesh, None, self._params())
             if rw.active:
@@ -719,11 +717,11 @@ class Domain:
     def _host_step_mixed(self):
         """One step of the mixed form when a boundary or an operator is a
         Python function of time: boundary values evaluated at the step's start
-        time for the first stage and at t + dt for the second RK2 stage (as
-        generic_domain.py:1974-2051), then every operator applied in
-        registration order with the step's timestep, at the time the
-        reference's operators see (the step's start for Euler, its end for
-        RK2)."""
+        time for the first stage, at t + dt for the second and (rk3) at
+        t + dt/2 for the third (as generic_domain.py:1974-2172), then every
+        operator applied in registration order with the step's timestep, at
+        the time the reference's operators see (the step's start for Euler,
+        its end otherwise)."""
         if any(f is not manning_friction_implicit for f in self.forcing_terms):
             raise NotImplementedError("the mixed form applies Manning friction only; other forcing terms run "
                                       "on precision='fp64'")
@@ -738,6 +736,9 @@ class Domain:
         dt = scn.step_begin()
         if host_bc and self.timestepping_method != "euler":
             self._bind_boundaries(self.starttime + t0 + dt)
+            if self.timestepping_method == "rk3":
+                scn.step_stage(2)
+                self._bind_boundaries(self.starttime + t0 + dt * 0.5)
         reason = self._take_stats(scn.step_end())
         t1 = self.relative_time
         if self.timestepping_method == "euler":

@@ -59,6 +59,7 @@ def lib():
             "agx_pool_deactivate": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_advance": ([H, P(ctypes.c_int32)], ctypes.c_int32),
             "agx_pool_step_begin": ([H], ctypes.c_int32),
+            "agx_pool_step_stage": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_step_end": ([H, P(ctypes.c_int32)], ctypes.c_int32),
             "agx_pool_get_stats": ([H, ctypes.c_int32, P(_lib.StepStats)], ctypes.c_int32),
             "agx_pool_operator_influx": ([H, ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
@@ -236,8 +237,12 @@ class Pool:
         """First stage of one step of every active scenario (see step_end)."""
         check(self.L.agx_pool_step_begin(self.h))
 
+    def step_stage(self, stage):
+        """Stage 2 or 3 of the split step on its own (after step_begin)."""
+        check(self.L.agx_pool_step_stage(self.h, int(stage)))
+
     def step_end(self):
-        """Second RK2 stage, step-loop operators and clocks; returns the
+        """The remaining stages, step-loop operators and clocks; returns the
         number of scenarios whose clock stopped."""
         n = ctypes.c_int32()
         check(self.L.agx_pool_step_end(self.h, ctypes.byref(n)))
@@ -400,6 +405,9 @@ class MixedScenario:
         self.pool.set_clock(self.sid, t, y, f, 1)
         self.pool.step_begin()
         return self.pool.stats(self.sid).last_timestep
+
+    def step_stage(self, stage):
+        self.pool.step_stage(stage)
 
     def step_end(self):
         self.pool.step_end()

@@ -109,6 +109,11 @@ agx_status agx_pool_advance(agx_pool p, int32_t* n_done);
  * gives each scenario's timestep; agx_pool_step_end runs the second stage,
  * the operators of the step loop and the clocks. */
 agx_status agx_pool_step_begin(agx_pool p);
+/* Runs stage 2, then (rk3 scenarios) stage 3 of the split step on its own,
+ * so that boundary values for the stage's time (t + dt, then t + dt/2) can
+ * be set before it; agx_pool_step_end runs the stages not run yet.
+ * AGX_E_STATE if called out of order. */
+agx_status agx_pool_step_stage(agx_pool p, int32_t stage);
 agx_status agx_pool_step_end(agx_pool p, int32_t* n_done);
 /* Continuous batching: up to max_steps more steps for every running scenario,
  * launched without waiting; agx_pool_wait completes it. */

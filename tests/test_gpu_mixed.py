@@ -80,10 +80,28 @@ def test_riverwall_depth_error_within_1mm(golden):
         assert np.abs(h - h_ref).max() <= DEPTH_TOL, (i, np.abs(h - h_ref).max())
 
 
-def test_rk3_is_refused_by_the_mixed_form():
-    d = workloads.dam_break(m=8, flow_algorithm="DE2", precision="mixed")
-    with pytest.raises(NotImplementedError, match="rk3"):
-        d._ensure_device()
+@pytest.mark.parametrize("name", ["traj_dambreak_de2", "traj_inflow_de2"])
+def test_rk3_depth_error_within_1mm(golden, name):
+    """DE2 (rk3: a third stage in the pool's step) against the reference's
+    trajectory."""
+    from anuga_core_gb300.mesh import rectangular_cross as rc
+    f = golden(name + ".npz")
+    m = int(f["mesh.m"])
+    L = float(f["mesh.points"][:, 0].max())
+    p, e, b = rc(m, m, L, L)
+    state = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"],
+                 elevation=f["init.elevation_c"], friction=f["init.friction"])
+    if "dambreak" in name:
+        kinds = {t: ("reflective", None) for t in ("left", "right", "top", "bottom")}
+    else:
+        kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
+                 "top": ("reflective", None), "bottom": ("reflective", None)}
+    d = make_domain(p, e, b, "DE2", state, kinds, precision="mixed")
+    z = f["init.elevation_c"]
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        h = np.maximum(d.quantities["stage"].centroid_values - z, 0.0)
+        h_ref = np.maximum(f["stage"][i] - z, 0.0)
+        assert np.abs(h - h_ref).max() <= DEPTH_TOL, (i, np.abs(h - h_ref).max())
 
 
 def test_dam_break_de0_depth_error_within_1mm(oracle_mod):

@@ -105,14 +105,15 @@ def test_rate_varying_in_time_matches_plain_within_1mm():
     assert abs(res["mixed"][1] - res["fp64"][1]) <= 1e-3 * abs(res["fp64"][1]) + 1e-9
 
 
-def test_time_function_boundary_matches_plain_within_1mm():
+@pytest.mark.parametrize("alg", ["DE1", "DE2"])
+def test_time_function_boundary_matches_plain_within_1mm(alg):
     """Time_boundary given as a function of time on the inflow edge: both
-    forms evaluate it at the step's start for the first stage and at t + dt
-    for the second RK2 stage (the mixed form between agx_pool_step_begin and
-    agx_pool_step_end)."""
+    forms evaluate it at the step's start for the first stage, at t + dt for
+    the second and (rk3) at t + dt/2 for the third (the mixed form between
+    agx_pool_step_begin, agx_pool_step_stage and agx_pool_step_end)."""
     res = {}
     for precision in ("fp64", "mixed"):
-        d = workloads.dam_break(m=24, flow_algorithm="DE1", precision=precision)
+        d = workloads.dam_break(m=24, flow_algorithm=alg, precision=precision)
         Br = agx.Reflective_boundary(d)
         Bt = agx.Time_boundary(d, function=lambda t: [0.8 + 0.2 * np.sin(0.5 * t), 0.0, 0.0])
         d.set_boundary({"left": Bt, "right": Br, "top": Br, "bottom": Br})
