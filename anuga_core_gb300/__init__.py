@@ -14,9 +14,15 @@ The user API mirrors the reference package names::
 from .mesh import Mesh, rectangular_cross
 from .domain import Domain, rectangular_cross_domain
 from .boundaries import (Reflective_boundary, Transmissive_boundary, Dirichlet_boundary, Time_boundary,
-                         Transmissive_n_momentum_zero_t_momentum_set_stage_boundary)
+                         Transmissive_n_momentum_zero_t_momentum_set_stage_boundary,
+                         Transmissive_momentum_set_stage_boundary, Transmissive_stage_zero_momentum_boundary,
+                         Time_stage_zero_momentum_boundary, Dirichlet_discharge_boundary,
+                         Flather_external_stage_zero_velocity_boundary)
 from .operators import Inlet_operator, Rate_operator
 
 __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "Reflective_boundary",
            "Transmissive_boundary", "Dirichlet_boundary", "Time_boundary",
-           "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Rate_operator", "Inlet_operator"]
+           "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Transmissive_momentum_set_stage_boundary",
+           "Transmissive_stage_zero_momentum_boundary", "Time_stage_zero_momentum_boundary",
+           "Dirichlet_discharge_boundary", "Flather_external_stage_zero_velocity_boundary",
+           "Rate_operator", "Inlet_operator"]

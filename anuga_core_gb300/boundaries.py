@@ -8,6 +8,11 @@ Same constructors as the reference:
 * ``Time_boundary(domain, function)``  generic_boundary_conditions.py:297-416
 * ``Transmissive_n_momentum_zero_t_momentum_set_stage_boundary(domain, function)``
   shallow_water/boundaries.py:384-519
+* ``Transmissive_momentum_set_stage_boundary(domain, function)``  boundaries.py:295-383
+* ``Transmissive_stage_zero_momentum_boundary(domain)``          boundaries.py:520-552
+* ``Time_stage_zero_momentum_boundary(domain, function)``        boundaries.py:553-638
+* ``Dirichlet_discharge_boundary(domain, stage0, wh0)``           boundaries.py:850-901
+* ``Flather_external_stage_zero_velocity_boundary(domain, function)`` boundaries.py:1096-1330
 
 Each evaluates on the device.  Time-dependent boundaries given as a Python
 function are sampled at the device time of every stage by the host-driven
@@ -118,3 +123,117 @@ class Transmissive_n_momentum_zero_t_momentum_set_stage_boundary(Boundary):
     def values(self, t):
         w = float(self.function(t)) if self.function is not None else float(self.stage or 0.0)
         return (w, 0.0, 0.0)
+
+
+def _stage_value(v):
+    # a stage function may return a number or a vector whose first entry is the stage
+    try:
+        return float(v)
+    except TypeError:
+        return float(np.asarray(v, float).ravel()[0])
+
+
+class Transmissive_momentum_set_stage_boundary(Boundary):
+    """Stage from f(t) (or a constant), both momenta transmitted from the
+    interior edge."""
+    kind = _lib.BC_TRANSMISSIVE_SET_STAGE
+
+    def __init__(self, domain=None, function=None):
+        if domain is None:
+            raise Exception("Domain must be specified for this type boundary")
+        if function is None:
+            raise Exception("Function must be specified for this type boundary")
+        self.domain = domain
+        self.function = function
+        self.device_loop = not callable(function)
+
+    def values(self, t):
+        w = _stage_value(self.function(t) if callable(self.function) else self.function)
+        return (w, 0.0, 0.0)
+
+    def __repr__(self):
+        return "Transmissive_momentum_set_stage_boundary(%s)" % self.domain
+
+
+class Transmissive_stage_zero_momentum_boundary(Boundary):
+    """Stage transmitted from the interior edge, momenta zero."""
+    kind = _lib.BC_TRANSMISSIVE_ZERO_MOM
+
+    def __init__(self, domain=None):
+        if domain is None:
+            raise Exception("Domain must be specified for Transmissive_stage_zero_momentum boundary")
+        self.domain = domain
+
+    def __repr__(self):
+        return "Transmissive_stage_zero_momentum_boundary(%s)" % self.domain
+
+
+class Time_stage_zero_momentum_boundary(Boundary):
+    """Stage from f(t), momenta zero (a Dirichlet value the host evaluates at
+    every stage's time).  The reference's class stores the function as
+    ``self.f`` but reads ``self.function`` when evaluated; this one applies
+    the documented behaviour."""
+    kind = _lib.BC_DIRICHLET
+    device_loop = False
+
+    def __init__(self, domain=None, function=None, default_boundary=None, verbose=False):
+        if domain is None:
+            raise Exception("You must specify a domain to Time_stage_zero_momemtum_boundary")
+        if function is None:
+            raise Exception("You must specify a function to Time_stage_zero_momemtum_boundary")
+        try:
+            q = float(function(0.0))
+        except Exception as e:
+            raise Exception("Function for time stage boundary could not be executed:\n%s" % e)
+        self.domain = domain
+        self.function = function
+        self.default_boundary = default_boundary
+
+    def values(self, t):
+        return (_stage_value(self.function(t)), 0.0, 0.0)
+
+    def __repr__(self):
+        return "Time_stage_zero_momemtum_boundary"
+
+
+class Dirichlet_discharge_boundary(Boundary):
+    """Stage stage0 and momentum wh0 along the inward normal of each edge."""
+    kind = _lib.BC_DIRICHLET
+
+    def __init__(self, domain=None, stage0=None, wh0=None):
+        if domain is None:
+            raise Exception("Domain must be specified for this type of boundary")
+        if stage0 is None:
+            raise Exception("Stage must be specified for this type of boundary")
+        self.domain = domain
+        self.stage0 = stage0
+        self.wh0 = 0.0 if wh0 is None else wh0
+
+    def edge_values(self, t, n1, n2):
+        """Values of edges with outward normals (n1, n2): [stage0, -wh0 n1, -wh0 n2]."""
+        return np.column_stack([np.full(n1.shape, float(self.stage0)), -self.wh0 * n1, -self.wh0 * n2])
+
+    def __repr__(self):
+        return "Dirichlet_Discharge_boundary(%s)" % self.domain
+
+
+class Flather_external_stage_zero_velocity_boundary(Boundary):
+    """Outside stage from f(t) and zero outside velocity combined with the
+    inside state along the characteristics (a weakly reflecting boundary)."""
+    kind = _lib.BC_FLATHER
+
+    def __init__(self, domain=None, function=None):
+        if domain is None:
+            raise Exception("Domain must be specified for this type boundary")
+        if function is None:
+            raise Exception("Function must be specified for this type boundary")
+        self.domain = domain
+        self.function = function
+        self.device_loop = not callable(function)
+
+    def values(self, t):
+        w = _stage_value(self.function(t) if callable(self.function) else self.function)
+        return (w, 0.0, 0.0)
+
+    def __repr__(self):
+        return "Flather_external_stage_zero_velocity_boundary(%s)" % self.domain

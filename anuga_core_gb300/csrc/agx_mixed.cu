@@ -455,6 +455,41 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
               uhr = P.velocity_extrapolation ? rk.y * rk.x : rk.y;
               vhr = P.velocity_extrapolation ? rk.z * rk.x : rk.z;
               break;
+            case BK_TRANSMISSIVE_SET_STAGE:
+              hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
+              uhr = L.uh;
+              vhr = L.vh;
+              break;
+            case BK_TRANSMISSIVE_ZERO_MOM:
+              hre = fmaxf(L.h, 0.0f);
+              uhr = 0.0f;
+              vhr = 0.0f;
+              break;
+            case BK_FLATHER: {
+              // heights relative to the cell's centroid bed (boundaries.py:1242-1330)
+              const float so = (float)(bv[0] - d.z[k]);
+              const float win = L.h + L.dz;               // edge stage - centroid bed
+              const float depth = fmaxf(win, 0.0f);
+              float q0;
+              if (depth == 0.0f || so > 0.0f) {
+                q0 = so >= 0.0f ? so : L.dz;
+                uhr = 0.0f;
+                vhr = 0.0f;
+              } else {
+                const float sg = sqrtf(P.g / depth);
+                const float ndotq = n1 * L.uh + n2 * L.vh;
+                const float w1 = -sg * so;
+                const float w2 = ndotq > 0.0f ? (n2 * L.uh - n1 * L.vh) / depth : 0.0f;
+                const float w3 = ndotq / depth + sg * win;
+                q0 = (w3 - w1) / (2.0f * sg);
+                const float qperp = 0.5f * (w3 + w1) * depth;
+                const float qpar = w2 * depth;
+                uhr = qperp * n1 + qpar * n2;
+                vhr = qperp * n2 - qpar * n1;
+              }
+              hre = fmaxf(q0 - L.dz, 0.0f);
+              break;
+            }
             case BK_TRANSMISSIVE_N0: {
               hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
               const float nq = n1 * L.uh + n2 * L.vh;
@@ -1650,6 +1685,9 @@ agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, c
   ScnHost& sh = p->scn[sid];
   if (B != sh.B) return pfail(AGX_E_INVALID, "boundary arrays need %d entries", sh.B);
   if (B == 0) return AGX_OK;
+  for (int64_t i = 0; i < B; i++)
+    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_FLATHER)
+      return pfail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
   PCK(cudaMemcpyAsync((void*)(p->d.bkind + sh.bnd0), kind, B * 4, cudaMemcpyHostToDevice, p->stream));
   if (values) PCK(cudaMemcpyAsync((void*)(p->d.bval + 3 * (size_t)sh.bnd0), values, B * 24, cudaMemcpyHostToDevice, p->stream));
   return psync(p);

@@ -160,8 +160,8 @@ __global__ void k_bc(Dev d, double t_override, double frac) {
     val = tv;
   }
   double wb, uhb, vhb;
-  boundary_value(kind, d.normals[2 * s], d.normals[2 * s + 1], d.we[s], d.uhe[s], d.vhe[s], d.w[k],
-                 d.uh[k], d.vh[k], val, wb, uhb, vhb);
+  boundary_value(kind, d.normals[2 * s], d.normals[2 * s + 1], d.we[s], d.uhe[s], d.vhe[s], d.ze[s], d.w[k],
+                 d.uh[k], d.vh[k], d.z[k], d.P.g, val, wb, uhb, vhb);
   d.wb[m] = wb;
   d.uhb[m] = uhb;
   d.vhb[m] = vhb;

@@ -88,6 +88,9 @@ enum BoundaryKind : int {
   BK_DIRICHLET = 4,       // constant (w, uh, vh)
   BK_TIME_SERIES = 5,     // piecewise-linear table of (t, w, uh, vh)
   BK_TRANSMISSIVE_N0 = 6, // transmissive stage/normal momentum, zero tangential
+  BK_TRANSMISSIVE_SET_STAGE = 7,  // stage given, momenta of the edge
+  BK_TRANSMISSIVE_ZERO_MOM = 8,   // stage of the edge, momenta zero
+  BK_FLATHER = 9,                 // outside stage given, zero outside velocity (characteristics)
 };
 
 // ---- per-cell meta bits (conn.w) -----------------------------------------
@@ -639,10 +642,37 @@ AGX_HD void accum_cell(const Params& P, int k, const int4& c, const SlotResult R
 }
 
 // ---- boundary values --------------------------------------------------------
-AGX_HD void boundary_value(int kind, double n1, double n2, double we, double uhe, double vhe,
-                           double wc, double uhc, double vhc, const double* val, double& wb,
+AGX_HD void boundary_value(int kind, double n1, double n2, double we, double uhe, double vhe, double ze,
+                           double wc, double uhc, double vhc, double zc, double g, const double* val, double& wb,
                            double& uhb, double& vhb) {
   switch (kind) {
+    case BK_TRANSMISSIVE_SET_STAGE:   // shallow_water/boundaries.py:295-383
+      wb = val[0]; uhb = uhe; vhb = vhe;
+      break;
+    case BK_TRANSMISSIVE_ZERO_MOM:    // boundaries.py:520-552
+      wb = we; uhb = 0.0; vhb = 0.0;
+      break;
+    case BK_FLATHER: {                // boundaries.py:1242-1330 (the vectorised form)
+      const double so = val[0];
+      const double depth = dmax(we - zc, 0.0);
+      if (!dnz(depth) || dgt(so, zc)) {
+        wb = dle(zc, so) ? so : ze;
+        uhb = 0.0 * uhe;
+        vhb = 0.0 * vhe;
+      } else {
+        const double sg = sqrt(g / depth);
+        const double ndotq = n1 * uhe + n2 * vhe;
+        const double w1 = 0.0 - sg * so;
+        const double w2 = dgt0(ndotq) ? (n2 * uhe - n1 * vhe) / depth : 0.0 * ndotq;
+        const double w3 = ndotq / depth + sg * we;
+        wb = (w3 - w1) / (2.0 * sg);
+        const double qperp = (w3 + w1) / 2.0 * depth;
+        const double qpar = w2 * depth;
+        uhb = qperp * n1 + qpar * n2;
+        vhb = qperp * n2 - qpar * n1;
+      }
+      break;
+    }
     case BK_REFLECTIVE: {
       wb = we;
       const double q1 = uhe, q2 = vhe;

@@ -485,7 +485,12 @@ class Domain:
                 if series is not None and not np.array_equal(series, B.series):
                     raise NotImplementedError("one time series per domain is supported")
                 series = B.series
-            elif k in (_lib.BC_DIRICHLET, _lib.BC_TRANSMISSIVE_N0):
+            elif hasattr(B, "edge_values"):
+                m = self.mesh
+                s = 3 * np.asarray(m.boundary_cells)[ids] + np.asarray(m.boundary_edges)[ids]
+                nrm = np.asarray(m.normals).reshape(-1, 2)
+                vals[ids] = B.edge_values(t, nrm[s, 0], nrm[s, 1])
+            elif k in (_lib.BC_DIRICHLET, _lib.BC_TRANSMISSIVE_N0, _lib.BC_TRANSMISSIVE_SET_STAGE, _lib.BC_FLATHER):
                 vals[ids] = B.values(t)
         return kind, vals, series
 

@@ -95,6 +95,10 @@ enum {
 #define AGX_BC_TRANSMISSIVE_C  3  /* same, centroid_transmissive_bc */
 #define AGX_BC_DIRICHLET       4  /* generic_boundary_conditions.py:221-264 */
 #define AGX_BC_TIME_SERIES     5  /* Time_boundary as a piecewise-linear table (generic_boundary_conditions.py:297-416) */
+#define AGX_BC_TRANSMISSIVE_N0 6  /* stage given, normal momentum of the edge, tangential zero (shallow_water/boundaries.py:384-519) */
+#define AGX_BC_TRANSMISSIVE_SET_STAGE 7  /* stage given, momenta of the edge (boundaries.py:295-383) */
+#define AGX_BC_TRANSMISSIVE_ZERO_MOM  8  /* stage of the edge, momenta zero (boundaries.py:520-552) */
+#define AGX_BC_FLATHER         9  /* outside stage given, zero outside velocity (boundaries.py:1096-1330) */
 
 /* Per-step statistics returned by agx_advance (generic_domain.py:1200
  * timestepping_statistics and the evolve bookkeeping). */

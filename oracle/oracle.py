@@ -340,7 +340,66 @@ class OracleDomain:
                 w, uh, vh = (float(v) for v in vals)
                 L.orc_bc_dirichlet(self.Dp, _p(ids), ids.size, w, uh, vh)
             else:
-                raise ValueError("unknown boundary kind %r" % kind)
+                self._bc_numpy(ids, kind, vals)
+
+    def _stage_of(self, f):
+        # a function of time giving the stage (or a vector whose first entry is)
+        v = f(self.starttime + self.relative_time) if callable(f) else f
+        try:
+            return float(v)
+        except TypeError:
+            return float(v[0])
+
+    def _bc_numpy(self, ids, kind, vals):
+        """The stage/momentum boundaries of shallow_water/boundaries.py,
+        restated on the boundary slots ``ids``."""
+        k = self.boundary_cells[ids]
+        e = self.boundary_edges[ids]
+        s = 3 * k + e
+        n1 = self.normals[2 * s]
+        n2 = self.normals[2 * s + 1]
+        if kind == "transmissive_set_stage":      # boundaries.py:295-383
+            self.stage_b[ids] = self._stage_of(vals)
+            self.xmom_b[ids] = self.xmom_e[s]
+            self.ymom_b[ids] = self.ymom_e[s]
+        elif kind == "transmissive_zero_momentum":  # boundaries.py:520-552
+            self.stage_b[ids] = self.stage_e[s]
+            self.xmom_b[ids] = 0.0
+            self.ymom_b[ids] = 0.0
+        elif kind == "time_stage_zero_momentum":  # boundaries.py:553-638 (stage f(t), momenta 0)
+            self.stage_b[ids] = self._stage_of(vals)
+            self.xmom_b[ids] = 0.0
+            self.ymom_b[ids] = 0.0
+        elif kind == "dirichlet_discharge":       # boundaries.py:850-901
+            stage0, wh0 = vals
+            self.stage_b[ids] = stage0
+            self.xmom_b[ids] = -wh0 * n1
+            self.ymom_b[ids] = -wh0 * n2
+        elif kind == "flather":                   # boundaries.py:1242-1330
+            stage_outside = self._stage_of(vals)
+            w_in, q1, q2 = self.stage_e[s], self.xmom_e[s], self.ymom_e[s]
+            z_edge = self.bed_e[s]
+            bed = self.bed_c[k]
+            depth_inside = np.maximum(w_in - bed, 0.0)
+            stage_out = 0.0 * w_in + stage_outside
+            q0_dry = np.where(bed <= stage_out, stage_out, z_edge)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                sg = (self.D.g / depth_inside) ** 0.5
+                ndotq = n1 * q1 + n2 * q2
+                w1 = 0.0 - sg * stage_out
+                w2 = np.where(ndotq > 0.0, (n2 * q1 - n1 * q2) / depth_inside, 0.0 * ndotq)
+                w3 = ndotq / depth_inside + sg * w_in
+                q0_wet = (w3 - w1) / (2.0 * sg)
+                qperp = (w3 + w1) / 2.0 * depth_inside
+                qpar = w2 * depth_inside
+                q1_wet = qperp * n1 + qpar * n2
+                q2_wet = qperp * n2 - qpar * n1
+            dry = np.logical_or(depth_inside == 0.0, stage_out > bed)
+            self.stage_b[ids] = np.where(dry, q0_dry, q0_wet)
+            self.xmom_b[ids] = np.where(dry, 0.0 * q1, q1_wet)
+            self.ymom_b[ids] = np.where(dry, 0.0 * q2, q2_wet)
+        else:
+            raise ValueError("unknown boundary kind %r" % kind)
 
     def compute_fluxes(self, substep):
         self.flux_timestep = lib().orc_compute_fluxes(self.Dp, substep, self.evolve_max_timestep)

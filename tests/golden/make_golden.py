@@ -243,6 +243,31 @@ def build_dam_break_riverwall(m=20):
     return d, extra
 
 
+def build_open_channel(m=16, n=8, L=160.0, W=80.0):
+    # a channel whose bed rises to the right under a 0.6 m water level; each
+    # side carries another of the stage/momentum boundaries of
+    # shallow_water/boundaries.py (Flather's outside stage below the bed at
+    # the right end, so that its wet branch is taken)
+    pts, elem, bnd = anuga.rectangular_cross(m, n, L, W)
+    d = anuga.Domain(pts, elem, bnd)
+    bed = lambda x, y: 0.55 * x / L + 0.02 * np.sin(y / 9.0)
+    d.set_quantity("elevation", bed)
+    d.set_quantity("stage", lambda x, y: np.maximum(0.6 + 0.0 * x, bed(x, y)))
+    d.set_quantity("friction", 0.025)
+    from anuga.shallow_water.boundaries import Dirichlet_discharge_boundary
+    d.set_boundary({
+        "left": anuga.Transmissive_momentum_set_stage_boundary(d, function=lambda t: 0.6 + 0.03 * np.sin(0.3 * t)),
+        "right": anuga.Flather_external_stage_zero_velocity_boundary(d, function=lambda t: 0.56 + 0.0 * t),
+        "top": Dirichlet_discharge_boundary(d, stage0=0.6, wh0=0.01),
+        "bottom": anuga.Transmissive_stage_zero_momentum_boundary(d)})
+    return d, {"mesh.points": pts, "mesh.elements": elem, "mesh.m": np.array(m), "mesh.n": np.array(n)}
+
+
+def boundary_fixtures():
+    trajectory_fixture("traj_channel_boundaries_de1.npz", build_open_channel, "DE1", 2.0, 12.0)
+    trajectory_fixture("traj_channel_boundaries_de0.npz", build_open_channel, "DE0", 2.0, 8.0)
+
+
 def flow_algorithm_fixtures():
     # the other flow algorithms of the DE family (shallow_water_domain.py:708-877):
     # DE2 (rk3 time stepping), DE0_7 and DE1_7 (other betas, minimum height)
@@ -256,6 +281,8 @@ if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "flows":
     flow_algorithm_fixtures()
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "boundaries":
+    boundary_fixtures()
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "riverwall":
     trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)
 elif __name__ == "__main__":
@@ -271,3 +298,4 @@ elif __name__ == "__main__":
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
     flow_algorithm_fixtures()
     trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)
+    boundary_fixtures()

@@ -80,6 +80,28 @@ def test_riverwall_depth_error_within_1mm(golden):
         assert np.abs(h - h_ref).max() <= DEPTH_TOL, (i, np.abs(h - h_ref).max())
 
 
+def test_channel_boundaries_depth_error_within_1mm(golden):
+    """The four stage/momentum boundaries of the channel case (Flather in its
+    wet branch) on the mixed form against the reference's trajectory."""
+    from anuga_core_gb300.mesh import rectangular_cross as rc
+    import anuga_core_gb300 as agx
+    f = golden("traj_channel_boundaries_de1.npz")
+    p, e, b = rc(int(f["mesh.m"]), int(f["mesh.n"]), 160.0, 80.0)
+    state = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"],
+                 elevation=f["init.elevation_c"], friction=f["init.friction"])
+    d = make_domain(p, e, b, "DE1", state, {t: ("reflective", None) for t in ("left", "right", "top", "bottom")},
+                    precision="mixed")
+    d.set_boundary({"left": agx.Transmissive_momentum_set_stage_boundary(d, function=lambda t: 0.6 + 0.03 * np.sin(0.3 * t)),
+                    "right": agx.Flather_external_stage_zero_velocity_boundary(d, function=lambda t: 0.56 + 0.0 * t),
+                    "top": agx.Dirichlet_discharge_boundary(d, stage0=0.6, wh0=0.01),
+                    "bottom": agx.Transmissive_stage_zero_momentum_boundary(d)})
+    z = f["init.elevation_c"]
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        h = np.maximum(d.quantities["stage"].centroid_values - z, 0.0)
+        h_ref = np.maximum(f["stage"][i] - z, 0.0)
+        assert np.abs(h - h_ref).max() <= DEPTH_TOL, (i, np.abs(h - h_ref).max())
+
+
 @pytest.mark.parametrize("name", ["traj_dambreak_de2", "traj_inflow_de2"])
 def test_rk3_depth_error_within_1mm(golden, name):
     """DE2 (rk3: a third stage in the pool's step) against the reference's

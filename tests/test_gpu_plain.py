@@ -348,6 +348,79 @@ def test_riverwall_trajectory_matches_reference(golden):
     assert np.abs(d2.quantities["stage"].centroid_values - f["stage"][-1]).max() > 1e-3
 
 
+def _channel_domain(f, alg, precision="fp64", constant=False):
+    m, n = int(f["mesh.m"]), int(f["mesh.n"])
+    p, e, b = rectangular_cross(m, n, 160.0, 80.0)
+    assert np.array_equal(p, f["mesh.points"])
+    state = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"],
+                 elevation=f["init.elevation_c"], friction=f["init.friction"])
+    d = make_domain(p, e, b, alg, state, {t: ("reflective", None) for t in ("left", "right", "top", "bottom")},
+                    precision=precision)
+    left = 0.6 if constant else (lambda t: 0.6 + 0.03 * np.sin(0.3 * t))
+    right = 0.56 if constant else (lambda t: 0.56 + 0.0 * t)
+    d.set_boundary({"left": agx.Transmissive_momentum_set_stage_boundary(d, function=left),
+                    "right": agx.Flather_external_stage_zero_velocity_boundary(d, function=right),
+                    "top": agx.Dirichlet_discharge_boundary(d, stage0=0.6, wh0=0.01),
+                    "bottom": agx.Transmissive_stage_zero_momentum_boundary(d)})
+    return d
+
+
+@pytest.mark.parametrize("alg", ["DE1", "DE0"])
+def test_channel_boundaries_match_reference(golden, alg):
+    """Transmissive_momentum_set_stage, Flather (wet branch), Dirichlet_discharge
+    and Transmissive_stage_zero_momentum boundaries against the reference."""
+    f = golden("traj_channel_boundaries_%s.npz" % alg.lower())
+    d = _channel_domain(f, alg)
+    steps = []
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        steps.append(d.number_of_steps)
+        Q = d.quantities
+        assert normwise(Q["stage"].centroid_values, f["stage"][i]) <= STATE_TOL, i
+        assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
+        assert normwise(Q["ymomentum"].centroid_values, f["ymom"][i]) <= 1e-10, i
+    assert steps == list(f["steps"])
+
+
+def test_channel_boundaries_in_the_device_loop(golden):
+    """Constant stages run in the device step loop; the same constants given
+    as functions run the host-driven step: bitwise the same."""
+    f = golden("traj_channel_boundaries_de1.npz")
+    out = []
+    for constant in (True, False):
+        d = _channel_domain(f, "DE1", constant=constant)
+        if not constant:   # functions returning the constants
+            d.boundary_map["left"].function = lambda t: 0.6
+            d.boundary_map["right"].function = lambda t: 0.56
+            d.boundary_map["left"].device_loop = d.boundary_map["right"].device_loop = False
+        for _ in d.evolve(yieldstep=2.0, finaltime=8.0):
+            pass
+        assert d._device_loop_ok() == constant
+        out.append((d.quantities["stage"].centroid_values.copy(), d.total_steps))
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][0], out[1][0])
+
+
+def test_time_stage_zero_momentum_matches_oracle(oracle_mod, golden):
+    f = golden("traj_channel_boundaries_de1.npz")
+    fn = lambda t: 0.6 + 0.05 * np.sin(0.2 * t)
+    d = _channel_domain(f, "DE1")
+    Br = agx.Reflective_boundary(d)
+    d.set_boundary({"left": agx.Time_stage_zero_momentum_boundary(d, function=fn), "right": Br, "top": Br,
+                    "bottom": Br})
+    kinds = {"left": ("time_stage_zero_momentum", fn), "right": ("reflective", None),
+             "top": ("reflective", None), "bottom": ("reflective", None)}
+    st = dict(stage=f["init.stage"], xmom=f["init.xmom"], ymom=f["init.ymom"], elevation=f["init.elevation_c"],
+              friction=f["init.friction"])
+    od = make_oracle(oracle_mod, d.mesh, "DE1", st, kinds)
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    for _ in d.evolve(yieldstep=2.0, finaltime=10.0):
+        pass
+    for _ in od.evolve(yieldstep=2.0, finaltime=10.0):
+        pass
+    assert d.total_steps == od.total_steps
+    assert normwise(d.quantities["stage"].centroid_values, od.stage_c) <= STATE_TOL
+
+
 def test_rk3_host_steps_equal_the_device_loop():
     """DE2 (rk3) through the per-phase host step (a rate given as a function
     of time) and through the device step loop (the same constant rate):

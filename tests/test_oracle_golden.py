@@ -141,3 +141,32 @@ def test_oracle_riverwall_trajectory_bit_exact(golden, oracle_mod):
         assert np.array_equal(r[2], f["stage"][i]), i
         assert np.array_equal(r[3], f["xmom"][i]), i
         assert np.array_equal(r[4], f["ymom"][i]), i
+
+
+CHANNEL = {"left": ("transmissive_set_stage", lambda t: 0.6 + 0.03 * np.sin(0.3 * t)),
+           "right": ("flather", lambda t: 0.56 + 0.0 * t),
+           "top": ("dirichlet_discharge", (0.6, 0.01)),
+           "bottom": ("transmissive_zero_momentum", None)}
+
+
+@pytest.mark.parametrize("alg", ["DE1", "DE0"])
+def test_oracle_channel_boundaries_bit_exact(golden, oracle_mod, alg):
+    """Transmissive_momentum_set_stage, Flather_external_stage_zero_velocity
+    (its wet branch), Dirichlet_discharge and Transmissive_stage_zero_momentum
+    boundaries, one per side of a channel, against the reference."""
+    f = golden("traj_channel_boundaries_%s.npz" % alg.lower())
+    m, n = int(f["mesh.m"]), int(f["mesh.n"])
+    p, e, b = rectangular_cross(m, n, 160.0, 80.0)
+    assert np.array_equal(p, f["mesh.points"])
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, alg)
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    od.set_boundaries([(M.tag_boundary_cells[t], CHANNEL[t][0], CHANNEL[t][1]) for t in M.tag_boundary_cells])
+    res = [(t, od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy(), od.ymom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[1] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[2], f["stage"][i]), i
+        assert np.array_equal(r[3], f["xmom"][i]), i
+        assert np.array_equal(r[4], f["ymom"][i]), i
