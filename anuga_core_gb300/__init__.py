@@ -17,7 +17,7 @@ from .boundaries import (Reflective_boundary, Transmissive_boundary, Dirichlet_b
                          Transmissive_n_momentum_zero_t_momentum_set_stage_boundary,
                          Transmissive_momentum_set_stage_boundary, Transmissive_stage_zero_momentum_boundary,
                          Time_stage_zero_momentum_boundary, Dirichlet_discharge_boundary,
-                         Flather_external_stage_zero_velocity_boundary)
+                         Flather_external_stage_zero_velocity_boundary, Characteristic_stage_boundary)
 from .operators import Inlet_operator, Rate_operator
 
 __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "Reflective_boundary",
@@ -25,4 +25,5 @@ __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "R
            "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Transmissive_momentum_set_stage_boundary",
            "Transmissive_stage_zero_momentum_boundary", "Time_stage_zero_momentum_boundary",
            "Dirichlet_discharge_boundary", "Flather_external_stage_zero_velocity_boundary",
+           "Characteristic_stage_boundary",
            "Rate_operator", "Inlet_operator"]

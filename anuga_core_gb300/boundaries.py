@@ -13,6 +13,7 @@ Same constructors as the reference:
 * ``Time_stage_zero_momentum_boundary(domain, function)``        boundaries.py:553-638
 * ``Dirichlet_discharge_boundary(domain, stage0, wh0)``           boundaries.py:850-901
 * ``Flather_external_stage_zero_velocity_boundary(domain, function)`` boundaries.py:1096-1330
+* ``Characteristic_stage_boundary(domain, function, default_stage)``   boundaries.py:639-848
 
 Each evaluates on the device.  Time-dependent boundaries given as a Python
 function are sampled at the device time of every stage by the host-driven
@@ -237,3 +238,26 @@ class Flather_external_stage_zero_velocity_boundary(Boundary):
 
     def __repr__(self):
         return "Flather_external_stage_zero_velocity_boundary(%s)" % self.domain
+
+
+class Characteristic_stage_boundary(Boundary):
+    """Stage from f(t); momentum of a simple incoming wave from the Riemann
+    invariant of the inside state."""
+    kind = _lib.BC_CHARACTERISTIC
+
+    def __init__(self, domain=None, function=None, default_stage=0.0):
+        if domain is None:
+            raise Exception("Domain must be specified for Characteristic_stage_boundary")
+        if function is None:
+            raise Exception("Function must be specified for Characteristic_stage_boundary")
+        self.domain = domain
+        self.function = function
+        self.default_stage = default_stage
+        self.device_loop = not callable(function)
+
+    def values(self, t):
+        w = _stage_value(self.function(t) if callable(self.function) else self.function)
+        return (w, 0.0, 0.0)
+
+    def __repr__(self):
+        return "Characteristic_stage_boundary(%s)" % self.domain

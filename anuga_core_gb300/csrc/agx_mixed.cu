@@ -490,6 +490,30 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
               hre = fmaxf(q0 - L.dz, 0.0f);
               break;
             }
+            case BK_CHARACTERISTIC: {
+              // heights relative to the edge bed (boundaries.py:757-848)
+              const float ho = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
+              const float hi = fmaxf(L.h, 0.0f);
+              if (hi == 0.0f || ho == 0.0f) {
+                hre = ho;
+                uhr = 0.0f;
+                vhr = 0.0f;
+              } else {
+                const float sqrt_g = sqrtf(P.g);
+                const float uh_in = n1 * L.uh + n2 * L.vh;
+                const float vh_in = n2 * L.uh - n1 * L.vh;
+                const float u_in = uh_in / hi;
+                const float si = sqrtf(hi), so = sqrtf(ho);
+                float h_m = 0.5f * (si + so) + 0.25f * u_in / sqrt_g;
+                h_m = h_m * h_m;
+                const float uh_m = h_m * (0.5f * u_in + sqrt_g * (si - so));
+                const float vh_m = uh_in > 0.0f ? vh_in : 0.0f;
+                hre = h_m;
+                uhr = uh_m * n1 + vh_m * n2;
+                vhr = uh_m * n2 - vh_m * n1;
+              }
+              break;
+            }
             case BK_TRANSMISSIVE_N0: {
               hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
               const float nq = n1 * L.uh + n2 * L.vh;
@@ -1686,7 +1710,7 @@ agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, c
   if (B != sh.B) return pfail(AGX_E_INVALID, "boundary arrays need %d entries", sh.B);
   if (B == 0) return AGX_OK;
   for (int64_t i = 0; i < B; i++)
-    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_FLATHER)
+    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_CHARACTERISTIC)
       return pfail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
   PCK(cudaMemcpyAsync((void*)(p->d.bkind + sh.bnd0), kind, B * 4, cudaMemcpyHostToDevice, p->stream));
   if (values) PCK(cudaMemcpyAsync((void*)(p->d.bval + 3 * (size_t)sh.bnd0), values, B * 24, cudaMemcpyHostToDevice, p->stream));

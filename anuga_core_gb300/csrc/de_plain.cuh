@@ -91,6 +91,7 @@ enum BoundaryKind : int {
   BK_TRANSMISSIVE_SET_STAGE = 7,  // stage given, momenta of the edge
   BK_TRANSMISSIVE_ZERO_MOM = 8,   // stage of the edge, momenta zero
   BK_FLATHER = 9,                 // outside stage given, zero outside velocity (characteristics)
+  BK_CHARACTERISTIC = 10,         // stage given, momentum of a simple incoming wave (Riemann invariant)
 };
 
 // ---- per-cell meta bits (conn.w) -----------------------------------------
@@ -652,6 +653,31 @@ AGX_HD void boundary_value(int kind, double n1, double n2, double we, double uhe
     case BK_TRANSMISSIVE_ZERO_MOM:    // boundaries.py:520-552
       wb = we; uhb = 0.0; vhb = 0.0;
       break;
+    case BK_CHARACTERISTIC: {         // boundaries.py:757-848 (the vectorised form)
+      const double wo = val[0];
+      const double sqrt_g = sqrt(g);
+      const double h_in = dmax(we - ze, 0.0);
+      const double h_out = dmax(wo - ze, 0.0);
+      if (!dnz(h_in) || !dnz(h_out)) {
+        wb = wo;
+        uhb = 0.0;
+        vhb = 0.0;
+      } else {
+        const double uh_in = n1 * uhe + n2 * vhe;
+        const double vh_in = n2 * uhe - n1 * vhe;
+        const double u_in = uh_in / h_in;
+        const double sh_in = sqrt(h_in), sh_out = sqrt(h_out);
+        double h_m = 0.5 * (sh_in + sh_out) + u_in / 4.0 / sqrt_g;
+        h_m = h_m * h_m;
+        const double u_m = 0.5 * u_in + sqrt_g * (sh_in - sh_out);
+        const double uh_m = h_m * u_m;
+        const double vh_m = dgt0(uh_in) ? vh_in : 0.0;
+        wb = h_m + ze;
+        uhb = uh_m * n1 + vh_m * n2;
+        vhb = uh_m * n2 - vh_m * n1;
+      }
+      break;
+    }
     case BK_FLATHER: {                // boundaries.py:1242-1330 (the vectorised form)
       const double so = val[0];
       const double depth = dmax(we - zc, 0.0);

@@ -99,6 +99,7 @@ enum {
 #define AGX_BC_TRANSMISSIVE_SET_STAGE 7  /* stage given, momenta of the edge (boundaries.py:295-383) */
 #define AGX_BC_TRANSMISSIVE_ZERO_MOM  8  /* stage of the edge, momenta zero (boundaries.py:520-552) */
 #define AGX_BC_FLATHER         9  /* outside stage given, zero outside velocity (boundaries.py:1096-1330) */
+#define AGX_BC_CHARACTERISTIC 10  /* stage given, incoming-wave momentum (boundaries.py:639-848) */
 
 /* Per-step statistics returned by agx_advance (generic_domain.py:1200
  * timestepping_statistics and the evolve bookkeeping). */

@@ -398,6 +398,29 @@ class OracleDomain:
             self.stage_b[ids] = np.where(dry, q0_dry, q0_wet)
             self.xmom_b[ids] = np.where(dry, 0.0 * q1, q1_wet)
             self.ymom_b[ids] = np.where(dry, 0.0 * q2, q2_wet)
+        elif kind == "characteristic":            # boundaries.py:757-848
+            w_outside = self._stage_of(vals)
+            w_in, q1, q2 = self.stage_e[s], self.xmom_e[s], self.ymom_e[s]
+            ze = self.bed_e[s]
+            w_out = 0.0 * w_in + w_outside
+            sqrt_g = self.D.g ** 0.5
+            h_in = np.maximum(w_in - ze, 0)
+            uh_in = n1 * q1 + n2 * q2
+            vh_in = n2 * q1 - n1 * q2
+            with np.errstate(divide="ignore", invalid="ignore"):
+                u_in = np.where(h_in > 0.0, uh_in / h_in, 0.0)
+            h_out = np.maximum(w_out - ze, 0)
+            sh_in = h_in ** 0.5
+            sh_out = h_out ** 0.5
+            h_m = (0.5 * (sh_in + sh_out) + u_in / 4.0 / sqrt_g) ** 2
+            u_m = 0.5 * u_in + sqrt_g * (sh_in - sh_out)
+            uh_m = h_m * u_m
+            vh_m = np.where(uh_in > 0.0, vh_in, 0.0)
+            w_m = h_m + ze
+            dry = np.logical_or(h_in == 0.0, h_out == 0.0)
+            self.stage_b[ids] = np.where(dry, w_out, w_m)
+            self.xmom_b[ids] = np.where(dry, 0.0, uh_m * n1 + vh_m * n2)
+            self.ymom_b[ids] = np.where(dry, 0.0, uh_m * n2 - vh_m * n1)
         else:
             raise ValueError("unknown boundary kind %r" % kind)
 

@@ -263,7 +263,16 @@ def build_open_channel(m=16, n=8, L=160.0, W=80.0):
     return d, {"mesh.points": pts, "mesh.elements": elem, "mesh.m": np.array(m), "mesh.n": np.array(n)}
 
 
+def build_characteristic_channel(m=16, n=8, L=160.0, W=80.0):
+    d, extra = build_open_channel(m, n, L, W)
+    d.set_boundary({"left": anuga.Characteristic_stage_boundary(d, function=lambda t: 0.6 + 0.03 * np.sin(0.3 * t)),
+                    "right": anuga.Transmissive_boundary(d), "top": anuga.Reflective_boundary(d),
+                    "bottom": anuga.Reflective_boundary(d)})
+    return d, extra
+
+
 def boundary_fixtures():
+    trajectory_fixture("traj_channel_characteristic_de1.npz", build_characteristic_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_boundaries_de1.npz", build_open_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_boundaries_de0.npz", build_open_channel, "DE0", 2.0, 8.0)
 

@@ -400,6 +400,26 @@ def test_channel_boundaries_in_the_device_loop(golden):
     assert np.array_equal(out[0][0], out[1][0])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_characteristic_boundary_matches_reference(golden, precision):
+    """Characteristic_stage_boundary on the inflow side: plain FP64 to the
+    trajectory tolerance, mixed within 1 mm of depth."""
+    f = golden("traj_channel_characteristic_de1.npz")
+    d = _channel_domain(f, "DE1", precision=precision)
+    d.set_boundary({"left": agx.Characteristic_stage_boundary(d, function=lambda t: 0.6 + 0.03 * np.sin(0.3 * t)),
+                    "right": agx.Transmissive_boundary(d), "top": agx.Reflective_boundary(d),
+                    "bottom": agx.Reflective_boundary(d)})
+    z = f["init.elevation_c"]
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        Q = d.quantities
+        if precision == "fp64":
+            assert normwise(Q["stage"].centroid_values, f["stage"][i]) <= STATE_TOL, i
+            assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
+        else:
+            err = np.abs(np.maximum(Q["stage"].centroid_values - z, 0) - np.maximum(f["stage"][i] - z, 0)).max()
+            assert err <= 1.0e-3, (i, err)
+
+
 def test_time_stage_zero_momentum_matches_oracle(oracle_mod, golden):
     f = golden("traj_channel_boundaries_de1.npz")
     fn = lambda t: 0.6 + 0.05 * np.sin(0.2 * t)

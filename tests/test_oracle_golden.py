@@ -170,3 +170,23 @@ def test_oracle_channel_boundaries_bit_exact(golden, oracle_mod, alg):
         assert np.array_equal(r[2], f["stage"][i]), i
         assert np.array_equal(r[3], f["xmom"][i]), i
         assert np.array_equal(r[4], f["ymom"][i]), i
+
+
+def test_oracle_characteristic_boundary_bit_exact(golden, oracle_mod):
+    """Characteristic_stage_boundary (shallow_water/boundaries.py:639-848)."""
+    f = golden("traj_channel_characteristic_de1.npz")
+    p, e, b = rectangular_cross(int(f["mesh.m"]), int(f["mesh.n"]), 160.0, 80.0)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, "DE1")
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    kinds = {"left": ("characteristic", lambda t: 0.6 + 0.03 * np.sin(0.3 * t)), "right": ("transmissive", None),
+             "top": R, "bottom": R}
+    od.set_boundaries([(M.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in M.tag_boundary_cells])
+    res = [(od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy(), od.ymom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[1], f["stage"][i]), i
+        assert np.array_equal(r[2], f["xmom"][i]), i
+        assert np.array_equal(r[3], f["ymom"][i]), i
