@@ -19,6 +19,7 @@ from .boundaries import (Reflective_boundary, Transmissive_boundary, Dirichlet_b
                          Time_stage_zero_momentum_boundary, Dirichlet_discharge_boundary,
                          Flather_external_stage_zero_velocity_boundary, Characteristic_stage_boundary)
 from .operators import Inlet_operator, Rate_operator
+from .checkpoint import load_checkpoint_file
 
 __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "Reflective_boundary",
            "Transmissive_boundary", "Dirichlet_boundary", "Time_boundary",
@@ -26,4 +27,4 @@ __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "R
            "Transmissive_stage_zero_momentum_boundary", "Time_stage_zero_momentum_boundary",
            "Dirichlet_discharge_boundary", "Flather_external_stage_zero_velocity_boundary",
            "Characteristic_stage_boundary",
-           "Rate_operator", "Inlet_operator"]
+           "Rate_operator", "Inlet_operator", "load_checkpoint_file"]

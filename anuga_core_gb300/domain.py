@@ -17,6 +17,8 @@ behind ``Quantity`` objects are mirrors refreshed on access.
 """
 from __future__ import annotations
 
+import os
+import pickle
 import time
 import warnings
 
@@ -804,8 +806,57 @@ class Domain:
         for t in self._evolve_base(yieldstep, finaltime, duration, skip_initial_step):
             if self.store and self.yieldstep_counter % self.output_frequency == 0:
                 self.store_timestep()
+            if getattr(self, "checkpoint", False):
+                self._maybe_checkpoint()
             yield t
             self.yieldstep_counter += 1
+
+    # ------------------------------------------------------------------
+    # checkpoint / resume (shallow_water_domain.py:1123-1157, :2376-2397;
+    # shallow_water/checkpoint.py)
+    def set_checkpointing(self, checkpoint=True, checkpoint_dir="CHECKPOINTS", checkpoint_step=10,
+                          checkpoint_time=None):
+        """Pickle the domain every ``checkpoint_step`` yieldsteps, or every
+        ``checkpoint_time`` wall-clock seconds if that is given, into
+        ``checkpoint_dir/<name>_<time>.pickle``; ``load_checkpoint_file``
+        restores it."""
+        if not checkpoint:
+            self.checkpoint = False
+            return
+        os.makedirs(checkpoint_dir, exist_ok=True)
+        self.checkpoint_dir = checkpoint_dir
+        if checkpoint_time is not None:
+            self.walltime_prev = time.time()
+            self.checkpoint_time = checkpoint_time
+            self.checkpoint_step = 0
+        else:
+            self.checkpoint_step = checkpoint_step
+        self.checkpoint = True
+
+    def _maybe_checkpoint(self):
+        if self.checkpoint_step == 0:
+            save = time.time() - self.walltime_prev > self.checkpoint_time
+        else:
+            save = self.yieldstep_counter % self.checkpoint_step == 0
+        if save:
+            name = os.path.join(self.checkpoint_dir, self.get_name()) + "_" + str(self.get_time()) + ".pickle"
+            with open(name, "wb") as fh:
+                pickle.dump(self, fh)
+            self.walltime_prev = time.time()
+
+    def __getstate__(self):
+        """The host state with every device field pulled; the device handle is
+        left out and made again (with the fields uploaded) on first use."""
+        if self._scn is not None:
+            self._pull([f for f in self._fstate])
+        state = self.__dict__.copy()
+        state["_scn"] = None
+        state["_scn_key"] = None
+        state["_fstate"] = {f: _SYNCED for f in self._fstate}
+        return state
+
+    def __setstate__(self, state):
+        self.__dict__.update(state)
 
     def _evolve_base(self, yieldstep, finaltime, duration, skip_initial_step):
         if self.boundary_map is None:

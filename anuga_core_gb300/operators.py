@@ -16,6 +16,21 @@ from .geometry import inside_polygon
 
 
 class Operator:
+    def __getstate__(self):
+        # a pickled operator (checkpoint) keeps the volume applied so far: the
+        # device counters start again from zero when the domain is restored
+        state = self.__dict__.copy()
+        total = None
+        if hasattr(self, "get_Q"):
+            total = self.get_Q()
+        elif hasattr(self, "get_total_applied_volume"):
+            total = self.get_total_applied_volume()
+        if total is not None:
+            state["_influx_offset"] = float(total)
+            if "cumulative_influx" in state:
+                state["cumulative_influx"] = 0.0
+        return state
+
     device_loop = True
 
     def __init__(self, domain):
@@ -67,8 +82,8 @@ class Rate_operator(Operator):
         """Cumulative influx (m^3) applied by this operator on the device."""
         d = self.domain
         if d._scn is not None and getattr(self, "_dev_index", None) is not None:
-            return d._scn.operator_influx(self._dev_index)
-        return self.cumulative_influx
+            return d._scn.operator_influx(self._dev_index) + getattr(self, "_influx_offset", 0.0)
+        return self.cumulative_influx + getattr(self, "_influx_offset", 0.0)
 
 
 def line_intersect(mesh, line):
@@ -181,5 +196,5 @@ class Inlet_operator(Operator):
     def get_total_applied_volume(self):
         d = self.domain
         if d._scn is not None and getattr(self, "_dev_index", None) is not None:
-            return d._scn.operator_influx(self._dev_index)
-        return 0.0
+            return d._scn.operator_influx(self._dev_index) + getattr(self, "_influx_offset", 0.0)
+        return getattr(self, "_influx_offset", 0.0)

@@ -41,19 +41,24 @@ class SWW_file:
         self._count = np.bincount(tri.ravel(), minlength=self.P).astype(float)
         self._count[self._count == 0] = 1.0
 
+    def __getstate__(self):
+        state = self.__dict__.copy()
+        state.pop("_bound_to", None)
+        return state
+
     def _device_frame(self):
         """(vertex [3, P], centroid [3, N]) float32 from the device, or None."""
         d = self.domain
         scn = d._scn
         if scn is None or not hasattr(scn, "sww_frame"):
             return None
-        if not getattr(self, "_bound", False):
+        if getattr(self, "_bound_to", None) is not scn:      # a new device scenario needs the node map
             slots = np.argsort(self._tri.ravel(), kind="stable")
             counts = np.bincount(self._tri.ravel(), minlength=self.P)
             off = np.zeros(self.P + 1, np.int64)
             off[1:] = np.cumsum(counts)
             scn.sww_bind(off, slots)
-            self._bound = True
+            self._bound_to = scn
         d._push_dirty()
         return scn.sww_frame(d.minimum_storable_height)
 
