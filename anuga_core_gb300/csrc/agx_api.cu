@@ -239,6 +239,7 @@ int64_t agx_scenario_footprint(int64_t n_cells, int64_t n_boundary, int64_t n_ed
 }
 
 agx_status agx_scenario_create(const agx_mesh_desc* m, const agx_params* p, agx_handle* out) {
+  AGX_TRACE("agx_scenario_create");
   if (!m || !p || !out) return fail(AGX_E_INVALID, "null argument");
   *out = nullptr;
   if (m->n_cells < 0 || m->n_cells >= (1ll << 29) || m->n_boundary < 0 || m->n_edges < 0)
@@ -356,6 +357,7 @@ agx_status agx_get_field(agx_handle h, int32_t f, double* host, int64_t n) {
 // The conserved centroid state (stage, xmomentum, ymomentum) in one call:
 // three copies on the scenario's stream and one synchronisation.
 agx_status agx_set_state(agx_handle h, const double* w, const double* uh, const double* vh, int64_t n) {
+  AGX_TRACE("agx_set_state");
   if (!h || !w || !uh || !vh) return fail(AGX_E_INVALID, "bad arguments");
   if (n != h->N) return fail(AGX_E_INVALID, "the state has %d cells, got %lld", h->N, (long long)n);
   if (n == 0) return AGX_OK;
@@ -366,6 +368,7 @@ agx_status agx_set_state(agx_handle h, const double* w, const double* uh, const 
 }
 
 agx_status agx_get_state(agx_handle h, double* w, double* uh, double* vh, int64_t n) {
+  AGX_TRACE("agx_get_state");
   if (!h || !w || !uh || !vh) return fail(AGX_E_INVALID, "bad arguments");
   if (n != h->N) return fail(AGX_E_INVALID, "the state has %d cells, asked for %lld", h->N, (long long)n);
   if (n == 0) return AGX_OK;
@@ -400,6 +403,7 @@ agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, co
 }
 
 agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out) {
+  AGX_TRACE("agx_sww_frame");
   if (!h || !vertex_out || !centroid_out) return fail(AGX_E_INVALID, "bad arguments");
   if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
   CK(enqueue_sww_frame(h, h->stream, min_storable_height));
@@ -484,6 +488,7 @@ agx_status agx_add_inlet_operator(agx_handle h, const int32_t* indices, int64_t 
 }
 
 agx_status agx_apply_operator(agx_handle h, int32_t op, double rate, double factor, double timestep) {
+  AGX_TRACE("agx_apply_operator");
   if (!h || op < 0 || op >= (int)h->ops.size() || !(timestep >= 0.0))
     return fail(AGX_E_INVALID, "bad operator %d or timestep", op);
   CK(enqueue_rate_once(h, h->stream, op, rate, factor, timestep));
@@ -510,6 +515,7 @@ agx_status agx_operator_influx(agx_handle h, int32_t op, double* influx) {
 }
 
 agx_status agx_protect(agx_handle h, double* mass_error) {
+  AGX_TRACE("agx_protect");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   agx_status st = pull_clock(h);
   if (st) return st;
@@ -521,18 +527,21 @@ agx_status agx_protect(agx_handle h, double* mass_error) {
 }
 
 agx_status agx_distribute(agx_handle h, int32_t with_protect) {
+  AGX_TRACE("agx_distribute");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   CK(enqueue_distribute(h, h->stream, with_protect != 0, true));
   return sync(h);
 }
 
 agx_status agx_update_boundary(agx_handle h, double t) {
+  AGX_TRACE("agx_update_boundary");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   CK(enqueue_boundary(h, h->stream, t, false));
   return sync(h);
 }
 
 agx_status agx_compute_fluxes(agx_handle h, int32_t substep, double* flux_timestep) {
+  AGX_TRACE("agx_compute_fluxes");
   if (!h || substep < 0 || substep > 2) return fail(AGX_E_INVALID, "bad arguments");
   CK(enqueue_fluxes(h, h->stream, substep));
   agx_status st = pull_clock(h);
@@ -557,12 +566,14 @@ agx_status agx_compute_fluxes(agx_handle h, int32_t substep, double* flux_timest
 }
 
 agx_status agx_compute_forcing(agx_handle h) {
+  AGX_TRACE("agx_compute_forcing");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   CK(enqueue_forcing(h, h->stream));
   return sync(h);
 }
 
 agx_status agx_update_conserved(agx_handle h, double timestep, int64_t* negative_cells) {
+  AGX_TRACE("agx_update_conserved");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   agx_status st = pull_clock(h);
   if (st) return st;
@@ -728,6 +739,7 @@ agx_status agx_get_stats(agx_handle h, agx_step_stats* out) {
 }
 
 agx_status agx_advance(agx_handle h, int64_t max_steps, agx_step_stats* out) {
+  AGX_TRACE("agx_advance");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   agx_status st = pull_clock(h);
   if (st) return st;

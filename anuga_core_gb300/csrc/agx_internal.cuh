@@ -1,6 +1,7 @@
 // agx_internal.cuh -- scenario object shared by the translation units of libagx.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string>
 #include <vector>
@@ -184,6 +185,17 @@ struct Scenario {
   int kernels_per_step = 0;
   void* rw_mem = nullptr;                // riverwall tables (one allocation)
 };
+
+// NVTX ranges around the library's entry points (a no-op unless a profiler
+// such as Nsight Systems is attached; generic_domain.py:47-54 wraps its step
+// phases the same way)
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
+#define AGX_TRACE(name) ::agx::TraceRange agx_trace_range_(name)
 
 // launch accounting
 void count_launch(int64_t n = 1);

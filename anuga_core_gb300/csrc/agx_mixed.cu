@@ -1300,6 +1300,7 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
                         const double* area, const int32_t* order, const int32_t* bcell, const int32_t* lnk,
                         const int32_t* halo_off, const int32_t* halo_cnt, int64_t n_halo,
                         const int32_t* halo_cells, const agx_params* prm, int32_t* sid_out) {
+  AGX_TRACE("agx_pool_add");
   if (!p || !conn || !geo || !area || !order || !prm || !sid_out || !lnk || !halo_off || !halo_cnt || N <= 0 ||
       B < 0 || n_halo < 0)
     return pfail(AGX_E_INVALID, "bad arguments");
@@ -1597,6 +1598,7 @@ __global__ void k_state_to_host(double* hw, double* huh, double* hvh, const doub
 // from page-locked host buffers, or else three copies through the staging
 // buffer and one permutation kernel.
 agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const double* uh, const double* vh, int64_t n) {
+  AGX_TRACE("agx_pool_set_state");
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !w || !uh || !vh)
     return pfail(AGX_E_INVALID, "bad arguments");
   ScnHost& sh = p->scn[sid];
@@ -1623,6 +1625,7 @@ agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const do
 }
 
 agx_status agx_pool_get_state(agx_pool p, int32_t sid, double* w, double* uh, double* vh, int64_t n) {
+  AGX_TRACE("agx_pool_get_state");
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !w || !uh || !vh)
     return pfail(AGX_E_INVALID, "bad arguments");
   ScnHost& sh = p->scn[sid];
@@ -1888,6 +1891,7 @@ agx_status agx_pool_operators_from_host(agx_pool p, int32_t sid, int32_t on) {
 
 agx_status agx_pool_apply_operator(agx_pool p, int32_t sid, int32_t op, double rate, double factor,
                                    double timestep) {
+  AGX_TRACE("agx_pool_apply_operator");
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
   ScnHost& sh = p->scn[sid];
   if (op < 0 || op >= (int)sh.ops.size() || !(timestep >= 0.0))
@@ -1978,6 +1982,7 @@ static void fill_stats_p(const Clock* c, agx_step_stats* o) {
 // Advance every active scenario until each reaches its yield time, final
 // time or step target.  One graph launch (device-side while loop).
 agx_status agx_pool_advance(agx_pool p, int32_t* n_done) {
+  AGX_TRACE("agx_pool_advance");
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   for (int s = 0; s < p->cap_scn; s++)
     if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
@@ -2004,6 +2009,7 @@ agx_status agx_pool_advance(agx_pool p, int32_t* n_done) {
 // One step split at the RK2 stages, without the graph (boundary values the
 // host evaluates at the second stage's time go in between).
 agx_status agx_pool_step_begin(agx_pool p) {
+  AGX_TRACE("agx_pool_step_begin");
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   for (int s = 0; s < p->cap_scn; s++)
     if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
@@ -2013,6 +2019,7 @@ agx_status agx_pool_step_begin(agx_pool p) {
 }
 
 agx_status agx_pool_step_stage(agx_pool p, int32_t stage) {
+  AGX_TRACE("agx_pool_step_stage");
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   if (stage != p->stages_done + 1 || stage < 2 || stage > 3)
     return pfail(AGX_E_STATE, "stage %d out of order (stage %d ran last)", stage, p->stages_done);
@@ -2022,6 +2029,7 @@ agx_status agx_pool_step_stage(agx_pool p, int32_t stage) {
 }
 
 agx_status agx_pool_step_end(agx_pool p, int32_t* n_done) {
+  AGX_TRACE("agx_pool_step_end");
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   if (p->stages_done < 1) return pfail(AGX_E_STATE, "agx_pool_step_begin has not run");
   for (int stage = p->stages_done + 1; stage <= 3; stage++) PCK(enqueue_later_stage(p, p->stream, stage));
@@ -2105,6 +2113,7 @@ int32_t agx_pool_grid(agx_pool p) { return p ? p->grid : 0; }
 // steps (stopping early at its final or yield time) and launch the device
 // loop without waiting.  agx_pool_wait completes the call.
 agx_status agx_pool_launch_chunk(agx_pool p, int64_t max_steps) {
+  AGX_TRACE("agx_pool_launch_chunk");
   if (!p || max_steps <= 0) return pfail(AGX_E_INVALID, "bad arguments");
   for (int s = 0; s < p->cap_scn; s++)
     if (p->scn[s].alive && p->scn[s].running) { agx_status st = ensure_work(p, s); if (st) return st; }
@@ -2130,6 +2139,7 @@ agx_status agx_pool_launch_chunk(agx_pool p, int64_t max_steps) {
 // Wait for the launched chunk; scenarios that reached their final time (or
 // failed) stop running.  Returns how many are still running.
 agx_status agx_pool_wait(agx_pool p, int32_t* n_running) {
+  AGX_TRACE("agx_pool_wait");
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   agx_status st = pull_scn(p);
   if (st) return st;
