@@ -329,21 +329,100 @@ __device__ float block_sum_f(float x, float* sh) {
   return r;
 }
 
+// Boundary kinds 7-10 (shallow_water/boundaries.py: stage given with the
+// edge's momenta, the edge's stage with zero momenta, Flather, the
+// characteristic stage boundary), out of line so that they take no
+// registers in the flux kernel where no edge has them.  Returns the outside
+// depth above the edge bed and the momenta; heights relative to the cell's
+// centroid bed zc (bv0: the boundary value of the stage).
+__device__ __noinline__ float3 boundary_state_rare(int kind, double bv0, double zc, EdgeState L, float n1, float n2,
+                                                   float g) {
+  float hre = 0.0f, uhr = 0.0f, vhr = 0.0f;
+  switch (kind) {
+    case BK_TRANSMISSIVE_SET_STAGE:
+      hre = fmaxf((float)(bv0 - zc) - L.dz, 0.0f);
+      uhr = L.uh;
+      vhr = L.vh;
+      break;
+    case BK_TRANSMISSIVE_ZERO_MOM:
+      hre = fmaxf(L.h, 0.0f);
+      uhr = 0.0f;
+      vhr = 0.0f;
+      break;
+    case BK_FLATHER: {
+      // heights relative to the cell's centroid bed (boundaries.py:1242-1330)
+      const float so = (float)(bv0 - zc);
+      const float win = L.h + L.dz;               // edge stage - centroid bed
+      const float depth = fmaxf(win, 0.0f);
+      float q0;
+      if (depth == 0.0f || so > 0.0f) {
+        q0 = so >= 0.0f ? so : L.dz;
+        uhr = 0.0f;
+        vhr = 0.0f;
+      } else {
+        const float sg = sqrtf(g / depth);
+        const float ndotq = n1 * L.uh + n2 * L.vh;
+        const float w1 = -sg * so;
+        const float w2 = ndotq > 0.0f ? (n2 * L.uh - n1 * L.vh) / depth : 0.0f;
+        const float w3 = ndotq / depth + sg * win;
+        q0 = (w3 - w1) / (2.0f * sg);
+        const float qperp = 0.5f * (w3 + w1) * depth;
+        const float qpar = w2 * depth;
+        uhr = qperp * n1 + qpar * n2;
+        vhr = qperp * n2 - qpar * n1;
+      }
+      hre = fmaxf(q0 - L.dz, 0.0f);
+      break;
+    }
+    case BK_CHARACTERISTIC: {
+      // heights relative to the edge bed (boundaries.py:757-848)
+      const float ho = fmaxf((float)(bv0 - zc) - L.dz, 0.0f);
+      const float hi = fmaxf(L.h, 0.0f);
+      if (hi == 0.0f || ho == 0.0f) {
+        hre = ho;
+        uhr = 0.0f;
+        vhr = 0.0f;
+      } else {
+        const float sqrt_g = sqrtf(g);
+        const float uh_in = n1 * L.uh + n2 * L.vh;
+        const float vh_in = n2 * L.uh - n1 * L.vh;
+        const float u_in = uh_in / hi;
+        const float si = sqrtf(hi), so = sqrtf(ho);
+        float h_m = 0.5f * (si + so) + 0.25f * u_in / sqrt_g;
+        h_m = h_m * h_m;
+        const float uh_m = h_m * (0.5f * u_in + sqrt_g * (si - so));
+        const float vh_m = uh_in > 0.0f ? vh_in : 0.0f;
+        hre = h_m;
+        uhr = uh_m * n1 + vh_m * n2;
+        vhr = uh_m * n2 - vh_m * n1;
+      }
+      break;
+    }
+    default:
+      break;
+  }
+  return make_float3(hre, uhr, vhr);
+}
+
 // ---------------------------------------------------------------------------
 // Fused flux kernel.  Phase 1 reconstructs the tile's own cells and its halo
 // cells (the outside neighbours its edges need) into shared memory; phase 2
 // evaluates the three edge fluxes of every own cell from shared memory and
 // accumulates them.  STG 1: first stage (explicit update and CFL minimum);
-// STG 2: second stage with the update and the combine fused in (RK2:
-// 0.5 Q + 0.5 Q0 into A; RK3: 0.25 Q + 0.75 Q0 into B); STG 3: third RK3
+// STG 2: second stage of the two-stage (RK2) scenarios with the update and
+// the combine 0.5 Q + 0.5 Q0 into A fused in; STG 4: second stage of the
+// three-stage (RK3) scenarios, 0.25 Q + 0.75 Q0 into B; STG 3: their third
 // stage, (2 Q + Q0) / 3 into A (generic_domain.py:1974-2172).
-template <int STG, int MINB, bool RW = false>
+// EXT: the extended form, launched only for pools with a riverwall or a
+// boundary of kinds 7-10 (riverwall weir branch, the rarer boundaries), so
+// that the common form carries none of their registers.
+template <int STG, int MINB, bool EXT = false>
 __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   constexpr bool FUSED2 = STG >= 2;
   __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
   __shared__ float shf[TILE / 32];
   __shared__ double shd[TILE / 32];
-  const float4* W = STG == 1 ? d.W0 : (STG == 2 ? d.W1 : d.W2);
+  const float4* W = STG == 1 ? d.W0 : (STG == 3 ? d.W2 : d.W1);
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
     const int base = tile * TILE;
     const int k = base + threadIdx.x;
@@ -357,7 +436,8 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
     PoolScn* S = d.scn + sid;
     if (!S->active) continue;
     if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
-    if (STG == 3 && !S->P.rk3) continue;      // RK2 scenarios have two
+    if (STG == 2 && S->P.rk3) continue;       // RK3 scenarios take STG 4 and 3
+    if (STG >= 3 && !S->P.rk3) continue;
     const MParams P = S->P;
     const bool valid = k < S->cell0 + S->ncell;
     bool sdry = false;
@@ -456,61 +536,18 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
               vhr = P.velocity_extrapolation ? rk.z * rk.x : rk.z;
               break;
             case BK_TRANSMISSIVE_SET_STAGE:
-              hre = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
-              uhr = L.uh;
-              vhr = L.vh;
-              break;
             case BK_TRANSMISSIVE_ZERO_MOM:
-              hre = fmaxf(L.h, 0.0f);
-              uhr = 0.0f;
-              vhr = 0.0f;
-              break;
-            case BK_FLATHER: {
-              // heights relative to the cell's centroid bed (boundaries.py:1242-1330)
-              const float so = (float)(bv[0] - d.z[k]);
-              const float win = L.h + L.dz;               // edge stage - centroid bed
-              const float depth = fmaxf(win, 0.0f);
-              float q0;
-              if (depth == 0.0f || so > 0.0f) {
-                q0 = so >= 0.0f ? so : L.dz;
-                uhr = 0.0f;
-                vhr = 0.0f;
-              } else {
-                const float sg = sqrtf(P.g / depth);
-                const float ndotq = n1 * L.uh + n2 * L.vh;
-                const float w1 = -sg * so;
-                const float w2 = ndotq > 0.0f ? (n2 * L.uh - n1 * L.vh) / depth : 0.0f;
-                const float w3 = ndotq / depth + sg * win;
-                q0 = (w3 - w1) / (2.0f * sg);
-                const float qperp = 0.5f * (w3 + w1) * depth;
-                const float qpar = w2 * depth;
-                uhr = qperp * n1 + qpar * n2;
-                vhr = qperp * n2 - qpar * n1;
-              }
-              hre = fmaxf(q0 - L.dz, 0.0f);
-              break;
-            }
+            case BK_FLATHER:
             case BK_CHARACTERISTIC: {
-              // heights relative to the edge bed (boundaries.py:757-848)
-              const float ho = fmaxf((float)(bv[0] - d.z[k]) - L.dz, 0.0f);
-              const float hi = fmaxf(L.h, 0.0f);
-              if (hi == 0.0f || ho == 0.0f) {
-                hre = ho;
+              if (EXT) {
+                const float3 q = boundary_state_rare(kind, bv[0], d.z[k], L, n1, n2, P.g);
+                hre = q.x;
+                uhr = q.y;
+                vhr = q.z;
+              } else {     // not reached: such pools run the extended form
+                hre = fmaxf(L.h, 0.0f);
                 uhr = 0.0f;
                 vhr = 0.0f;
-              } else {
-                const float sqrt_g = sqrtf(P.g);
-                const float uh_in = n1 * L.uh + n2 * L.vh;
-                const float vh_in = n2 * L.uh - n1 * L.vh;
-                const float u_in = uh_in / hi;
-                const float si = sqrtf(hi), so = sqrtf(ho);
-                float h_m = 0.5f * (si + so) + 0.25f * u_in / sqrt_g;
-                h_m = h_m * h_m;
-                const float uh_m = h_m * (0.5f * u_in + sqrt_g * (si - so));
-                const float vh_m = uh_in > 0.0f ? vh_in : 0.0f;
-                hre = h_m;
-                uhr = uh_m * n1 + vh_m * n2;
-                vhr = uh_m * n2 - vh_m * n1;
               }
               break;
             }
@@ -523,7 +560,8 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
             }
             case BK_TIME_SERIES: {
               double v3[3];
-              const double tnow = S->clock.time + (STG == 1 ? 0.0 : (STG == 2 ? 1.0 : 0.5)) * S->clock.timestep;
+              const double tnow = STG == 1 ? S->clock.time
+                                  : S->clock.time + (STG == 3 ? 0.5 : 1.0) * S->clock.timestep;
               series_at(S->series, S->nseries, tnow, v3);
               hre = fmaxf((float)(v3[0] - d.z[k]) - L.dz, 0.0f);
               uhr = (float)v3[1];
@@ -539,7 +577,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
           }
         }
         Flux32 F;
-        if (RW && ((cn.w >> (20 + i)) & 1)) {
+        if (EXT && ((cn.w >> (20 + i)) & 1)) {
           // riverwall edge (sw_domain_openmp.c:581-650), all heights relative
           // to this edge's bed zl: crest c, Audusse bed zh = max(0, zr - zl, c)
           const size_t q = 3 * (size_t)k + i;
@@ -593,7 +631,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         double h = sw, uh = suh, vh = svh;
         neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
                           S->clock.timestep32, added);
-        if (STG == 2 && !P.rk3) {
+        if (STG == 2) {
           h = half_sum(h, d.wA[k]);
           uh = half_sum(uh, d.uhA[k]);
           vh = half_sum(vh, d.vhA[k]);
@@ -601,7 +639,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
           d.uhA[k] = uh;
           d.vhA[k] = vh;
           d.W0[k] = record_of(P, h, uh, vh);     // work record of the next step
-        } else if (STG == 2) {                    // RK3: Q2 = 0.25 Q + 0.75 Q0 (depth-linear)
+        } else if (STG == 4) {                    // RK3: Q2 = 0.25 Q + 0.75 Q0 (depth-linear)
           h = 0.25 * h + 0.75 * d.wA[k];
           uh = 0.25 * uh + 0.75 * d.uhA[k];
           vh = 0.25 * vh + 0.75 * d.vhA[k];
@@ -973,6 +1011,7 @@ struct Pool {
   int kernels_per_iter = 0;
   int mode_rk2_any = 1;
   bool rw_any = false;           // some scenario has riverwalls: the flux kernels take the wall branch
+  bool rare_bc_any = false;      // some boundary has kind 7-10: the extended flux kernels run
   bool rk3_any = false;          // some scenario has three stages: the third-stage flux kernel runs
   int stages_done = 0;           // stages run by agx_pool_step_begin / _stage in the current split step
   void* w2_mem = nullptr;        // third-stage work records
@@ -1101,7 +1140,7 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
-  if (p->rw_any) k_pool_flux<1, 6, true><<<Gf, TILE, 0, st>>>(d);
+  if (p->rw_any || p->rare_bc_any) k_pool_flux<1, 6, true><<<Gf, TILE, 0, st>>>(d);
   else if (p->variant == 0) k_pool_flux<1, 6><<<Gf, TILE, 0, st>>>(d);
   else k_pool_flux<1, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
@@ -1124,11 +1163,17 @@ static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
   if (stage == 3 && !p->rk3_any) return cudaSuccess;
   if (stage == 2) {
-    if (p->rw_any) k_pool_flux<2, 6, true><<<Gf, TILE, 0, st>>>(d);
+    if (p->rw_any || p->rare_bc_any) k_pool_flux<2, 6, true><<<Gf, TILE, 0, st>>>(d);
     else if (p->variant == 0) k_pool_flux<2, 6><<<Gf, TILE, 0, st>>>(d);
     else k_pool_flux<2, 8><<<Gf, TILE, 0, st>>>(d);
+    if (p->rk3_any) {
+      count_launch();
+      if (p->rw_any || p->rare_bc_any) k_pool_flux<4, 6, true><<<Gf, TILE, 0, st>>>(d);
+      else if (p->variant == 0) k_pool_flux<4, 6><<<Gf, TILE, 0, st>>>(d);
+      else k_pool_flux<4, 8><<<Gf, TILE, 0, st>>>(d);
+    }
   } else {
-    if (p->rw_any) k_pool_flux<3, 6, true><<<Gf, TILE, 0, st>>>(d);
+    if (p->rw_any || p->rare_bc_any) k_pool_flux<3, 6, true><<<Gf, TILE, 0, st>>>(d);
     else if (p->variant == 0) k_pool_flux<3, 6><<<Gf, TILE, 0, st>>>(d);
     else k_pool_flux<3, 8><<<Gf, TILE, 0, st>>>(d);
   }
@@ -1712,9 +1757,16 @@ agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, c
   ScnHost& sh = p->scn[sid];
   if (B != sh.B) return pfail(AGX_E_INVALID, "boundary arrays need %d entries", sh.B);
   if (B == 0) return AGX_OK;
-  for (int64_t i = 0; i < B; i++)
+  bool rare = false;
+  for (int64_t i = 0; i < B; i++) {
     if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_CHARACTERISTIC)
       return pfail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
+    rare |= kind[i] >= AGX_BC_TRANSMISSIVE_SET_STAGE;
+  }
+  if (rare && !p->rare_bc_any) {
+    p->rare_bc_any = true;
+    p->graph_valid = false;
+  }
   PCK(cudaMemcpyAsync((void*)(p->d.bkind + sh.bnd0), kind, B * 4, cudaMemcpyHostToDevice, p->stream));
   if (values) PCK(cudaMemcpyAsync((void*)(p->d.bval + 3 * (size_t)sh.bnd0), values, B * 24, cudaMemcpyHostToDevice, p->stream));
   return psync(p);
