@@ -14,6 +14,7 @@ Same constructors as the reference:
 * ``Dirichlet_discharge_boundary(domain, stage0, wh0)``           boundaries.py:850-901
 * ``Flather_external_stage_zero_velocity_boundary(domain, function)`` boundaries.py:1096-1330
 * ``Characteristic_stage_boundary(domain, function, default_stage)``   boundaries.py:639-848
+* ``Time_space_boundary(domain, function(t, x, y))``  generic_boundary_conditions.py:419-517
 
 Each evaluates on the device.  Time-dependent boundaries given as a Python
 function are sampled at the device time of every stage by the host-driven
@@ -210,7 +211,7 @@ class Dirichlet_discharge_boundary(Boundary):
         self.stage0 = stage0
         self.wh0 = 0.0 if wh0 is None else wh0
 
-    def edge_values(self, t, n1, n2):
+    def edge_values(self, t, n1, n2, x, y):
         """Values of edges with outward normals (n1, n2): [stage0, -wh0 n1, -wh0 n2]."""
         return np.column_stack([np.full(n1.shape, float(self.stage0)), -self.wh0 * n1, -self.wh0 * n2])
 
@@ -261,3 +262,32 @@ class Characteristic_stage_boundary(Boundary):
 
     def __repr__(self):
         return "Characteristic_stage_boundary(%s)" % self.domain
+
+
+class Time_space_boundary(Boundary):
+    """Dirichlet values f(t, x, y) -> (w, uh, vh) at each edge's midpoint,
+    evaluated by the host at every stage's time."""
+    kind = _lib.BC_DIRICHLET
+    device_loop = False
+
+    def __init__(self, domain=None, function=None, default_boundary=None, verbose=False):
+        if function is None:
+            raise Exception("You must specify a function to Time_space_boundary")
+        try:
+            q = np.array(function(0.0, 0.0, 0.0), float)
+        except Exception as e:
+            raise Exception("Function for time_space_boundary could not be executed:\n%s" % e)
+        if q.size != 3:
+            raise Exception("Return value from time_space_boundary function must be a list of 3 values")
+        self.domain = domain
+        self.function = function
+        self.default_boundary = default_boundary
+
+    def edge_values(self, t, n1, n2, x, y):
+        out = np.empty((len(x), 3))
+        for i in range(len(x)):
+            out[i] = np.asarray(self.function(t, x[i], y[i]), float).ravel()[:3]
+        return out
+
+    def __repr__(self):
+        return "Time space boundary"

@@ -398,6 +398,13 @@ class OracleDomain:
             self.stage_b[ids] = np.where(dry, q0_dry, q0_wet)
             self.xmom_b[ids] = np.where(dry, 0.0 * q1, q1_wet)
             self.ymom_b[ids] = np.where(dry, 0.0 * q2, q2_wet)
+        elif kind == "time_space":                # generic_boundary_conditions.py:419-517
+            t = self.starttime + self.relative_time
+            x = self.edge_coordinates[2 * s]
+            y = self.edge_coordinates[2 * s + 1]
+            for j in range(len(ids)):
+                q = np.asarray(vals(t, x[j], y[j]), float).ravel()
+                self.stage_b[ids[j]], self.xmom_b[ids[j]], self.ymom_b[ids[j]] = q[0], q[1], q[2]
         elif kind == "characteristic":            # boundaries.py:757-848
             w_outside = self._stage_of(vals)
             w_in, q1, q2 = self.stage_e[s], self.xmom_e[s], self.ymom_e[s]

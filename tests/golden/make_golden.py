@@ -271,7 +271,20 @@ def build_characteristic_channel(m=16, n=8, L=160.0, W=80.0):
     return d, extra
 
 
+def _time_space(t, x, y):
+    return [0.6 + 0.02 * np.sin(0.3 * t) * np.cos(y / 20.0), 0.0, 0.0]
+
+
+def build_time_space_channel(m=16, n=8, L=160.0, W=80.0):
+    d, extra = build_open_channel(m, n, L, W)
+    d.set_boundary({"left": anuga.Time_space_boundary(d, function=_time_space),
+                    "right": anuga.Transmissive_boundary(d), "top": anuga.Reflective_boundary(d),
+                    "bottom": anuga.Reflective_boundary(d)})
+    return d, extra
+
+
 def boundary_fixtures():
+    trajectory_fixture("traj_channel_time_space_de1.npz", build_time_space_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_characteristic_de1.npz", build_characteristic_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_boundaries_de1.npz", build_open_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_boundaries_de0.npz", build_open_channel, "DE0", 2.0, 8.0)

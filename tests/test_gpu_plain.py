@@ -420,6 +420,18 @@ def test_characteristic_boundary_matches_reference(golden, precision):
             assert err <= 1.0e-3, (i, err)
 
 
+def test_time_space_boundary_matches_reference(golden):
+    f = golden("traj_channel_time_space_de1.npz")
+    d = _channel_domain(f, "DE1")
+    fn = lambda t, x, y: [0.6 + 0.02 * np.sin(0.3 * t) * np.cos(y / 20.0), 0.0, 0.0]
+    d.set_boundary({"left": agx.Time_space_boundary(d, function=fn), "right": agx.Transmissive_boundary(d),
+                    "top": agx.Reflective_boundary(d), "bottom": agx.Reflective_boundary(d)})
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        Q = d.quantities
+        assert normwise(Q["stage"].centroid_values, f["stage"][i]) <= STATE_TOL, i
+        assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
+
+
 def test_time_stage_zero_momentum_matches_oracle(oracle_mod, golden):
     f = golden("traj_channel_boundaries_de1.npz")
     fn = lambda t: 0.6 + 0.05 * np.sin(0.2 * t)

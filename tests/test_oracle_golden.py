@@ -190,3 +190,25 @@ def test_oracle_characteristic_boundary_bit_exact(golden, oracle_mod):
         assert np.array_equal(r[1], f["stage"][i]), i
         assert np.array_equal(r[2], f["xmom"][i]), i
         assert np.array_equal(r[3], f["ymom"][i]), i
+
+
+def _time_space(t, x, y):
+    return [0.6 + 0.02 * np.sin(0.3 * t) * np.cos(y / 20.0), 0.0, 0.0]
+
+
+def test_oracle_time_space_boundary_bit_exact(golden, oracle_mod):
+    """Time_space_boundary (generic_boundary_conditions.py:419-517)."""
+    f = golden("traj_channel_time_space_de1.npz")
+    p, e, b = rectangular_cross(int(f["mesh.m"]), int(f["mesh.n"]), 160.0, 80.0)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, "DE1")
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    kinds = {"left": ("time_space", _time_space), "right": ("transmissive", None), "top": R, "bottom": R}
+    od.set_boundaries([(M.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in M.tag_boundary_cells])
+    res = [(od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[1], f["stage"][i]), i
+        assert np.array_equal(r[2], f["xmom"][i]), i
