@@ -18,7 +18,7 @@ from .boundaries import (Reflective_boundary, Transmissive_boundary, Dirichlet_b
                          Transmissive_momentum_set_stage_boundary, Transmissive_stage_zero_momentum_boundary,
                          Time_stage_zero_momentum_boundary, Dirichlet_discharge_boundary,
                          Flather_external_stage_zero_velocity_boundary, Characteristic_stage_boundary,
-                         Time_space_boundary)
+                         Time_space_boundary, Inflow_boundary, Compute_fluxes_boundary)
 from .operators import Inlet_operator, Rate_operator
 from .checkpoint import load_checkpoint_file
 
@@ -27,5 +27,5 @@ __all__ = ["Mesh", "rectangular_cross", "Domain", "rectangular_cross_domain", "R
            "Transmissive_n_momentum_zero_t_momentum_set_stage_boundary", "Transmissive_momentum_set_stage_boundary",
            "Transmissive_stage_zero_momentum_boundary", "Time_stage_zero_momentum_boundary",
            "Dirichlet_discharge_boundary", "Flather_external_stage_zero_velocity_boundary",
-           "Characteristic_stage_boundary", "Time_space_boundary",
+           "Characteristic_stage_boundary", "Time_space_boundary", "Inflow_boundary", "Compute_fluxes_boundary",
            "Rate_operator", "Inlet_operator", "load_checkpoint_file"]

@@ -29,7 +29,7 @@ FIELDS = ["stage_c", "xmom_c", "ymom_c", "elev_c", "friction_c", "height_c",
 FIELD = {n: i for i, n in enumerate(FIELDS)}
 
 (BC_NONE, BC_REFLECTIVE, BC_TRANSMISSIVE, BC_TRANSMISSIVE_C, BC_DIRICHLET, BC_TIME_SERIES, BC_TRANSMISSIVE_N0,
- BC_TRANSMISSIVE_SET_STAGE, BC_TRANSMISSIVE_ZERO_MOM, BC_FLATHER, BC_CHARACTERISTIC) = range(11)
+ BC_TRANSMISSIVE_SET_STAGE, BC_TRANSMISSIVE_ZERO_MOM, BC_FLATHER, BC_CHARACTERISTIC, BC_INFLOW) = range(12)
 STOP_YIELD, STOP_FINAL, STOP_MAXSTEPS, STOP_ERROR = 1, 2, 3, 4
 PHASES = ("prep", "extrap", "bc", "flux", "accum", "update", "rate", "small")
 PHASE_COUNT = len(PHASES)

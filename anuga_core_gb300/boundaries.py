@@ -15,6 +15,8 @@ Same constructors as the reference:
 * ``Flather_external_stage_zero_velocity_boundary(domain, function)`` boundaries.py:1096-1330
 * ``Characteristic_stage_boundary(domain, function, default_stage)``   boundaries.py:639-848
 * ``Time_space_boundary(domain, function(t, x, y))``  generic_boundary_conditions.py:419-517
+* ``Inflow_boundary(domain, rate)``                  shallow_water/boundaries.py:902-992
+* ``Compute_fluxes_boundary()``                      generic_boundary_conditions.py:266-296
 
 Each evaluates on the device.  Time-dependent boundaries given as a Python
 function are sampled at the device time of every stage by the host-driven
@@ -211,7 +213,7 @@ class Dirichlet_discharge_boundary(Boundary):
         self.stage0 = stage0
         self.wh0 = 0.0 if wh0 is None else wh0
 
-    def edge_values(self, t, n1, n2, x, y):
+    def edge_values(self, t, n1, n2, x, y, tag=None):
         """Values of edges with outward normals (n1, n2): [stage0, -wh0 n1, -wh0 n2]."""
         return np.column_stack([np.full(n1.shape, float(self.stage0)), -self.wh0 * n1, -self.wh0 * n2])
 
@@ -283,7 +285,7 @@ class Time_space_boundary(Boundary):
         self.function = function
         self.default_boundary = default_boundary
 
-    def edge_values(self, t, n1, n2, x, y):
+    def edge_values(self, t, n1, n2, x, y, tag=None):
         out = np.empty((len(x), 3))
         for i in range(len(x)):
             out[i] = np.asarray(self.function(t, x[i], y[i]), float).ravel()[:3]
@@ -291,3 +293,50 @@ class Time_space_boundary(Boundary):
 
     def __repr__(self):
         return "Time space boundary"
+
+
+class Inflow_boundary(Boundary):
+    """A discharge ``rate`` (m^3/s) spread over the tag's edges: momentum
+    rate / (total edge length) along each inward normal, stage 1 m above the
+    edge's bed (the reference's Manning depth with a zero slope)."""
+    kind = _lib.BC_INFLOW
+
+    def __init__(self, domain=None, rate=0.0):
+        if domain is None:
+            raise Exception("Domain must be specified for Inflow boundary")
+        self.domain = domain
+        self.rate = rate
+        self.tag = None
+        self.length = None
+
+    def _tag_length(self, tag):
+        # the tag of the first edge evaluated fixes the length (the reference's cache)
+        if self.tag is None:
+            self.tag = tag
+            m = self.domain.mesh
+            length = 0.0
+            lengths = np.asarray(m.edgelengths).reshape(-1, 3)
+            for (v, e), t in m.boundary.items():
+                if t == self.tag:
+                    length += lengths[v, e]
+            self.length = length
+            self.average_momentum = self.rate / length
+        return self.average_momentum
+
+    def edge_values(self, t, n1, n2, x, y, tag=None):
+        mu = self._tag_length(tag)
+        return np.column_stack([np.full(n1.shape, 1.0), mu * (-n1), mu * (-n2)])
+
+    def __repr__(self):
+        return "Inflow_boundary(%s)" % self.domain
+
+
+class Compute_fluxes_boundary(Boundary):
+    """Leaves the boundary values as they are (the flux computation decides)."""
+    kind = _lib.BC_NONE
+
+    def __init__(self):
+        self.domain = None
+
+    def __repr__(self):
+        return "Compute_fluxes_boundary(%s)" % self.domain

@@ -423,7 +423,7 @@ agx_status agx_set_boundary(agx_handle h, const int32_t* kind, const double* val
   if (!h || B != h->B) return fail(AGX_E_INVALID, "boundary arrays must have B=%d entries", h ? h->B : -1);
   if (B == 0) return AGX_OK;
   for (int64_t i = 0; i < B; i++)
-    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_CHARACTERISTIC)
+    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_INFLOW)
       return fail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
   CK(cudaMemcpyAsync(h->bkind, kind, (size_t)B * 4, cudaMemcpyHostToDevice, h->stream));
   if (values) CK(cudaMemcpyAsync(h->bval, values, (size_t)B * 24, cudaMemcpyHostToDevice, h->stream));

@@ -335,10 +335,16 @@ __device__ float block_sum_f(float x, float* sh) {
 // registers in the flux kernel where no edge has them.  Returns the outside
 // depth above the edge bed and the momenta; heights relative to the cell's
 // centroid bed zc (bv0: the boundary value of the stage).
-__device__ __noinline__ float3 boundary_state_rare(int kind, double bv0, double zc, EdgeState L, float n1, float n2,
-                                                   float g) {
+__device__ __noinline__ float3 boundary_state_rare(int kind, const double* bv, double zc, EdgeState L, float n1,
+                                                   float n2, float g) {
   float hre = 0.0f, uhr = 0.0f, vhr = 0.0f;
+  const double bv0 = bv[0];
   switch (kind) {
+    case BK_INFLOW:                   // boundaries.py:902-992: a depth above the edge bed
+      hre = fmaxf((float)bv0, 0.0f);
+      uhr = (float)bv[1];
+      vhr = (float)bv[2];
+      break;
     case BK_TRANSMISSIVE_SET_STAGE:
       hre = fmaxf((float)(bv0 - zc) - L.dz, 0.0f);
       uhr = L.uh;
@@ -538,9 +544,10 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
             case BK_TRANSMISSIVE_SET_STAGE:
             case BK_TRANSMISSIVE_ZERO_MOM:
             case BK_FLATHER:
-            case BK_CHARACTERISTIC: {
+            case BK_CHARACTERISTIC:
+            case BK_INFLOW: {
               if (EXT) {
-                const float3 q = boundary_state_rare(kind, bv[0], d.z[k], L, n1, n2, P.g);
+                const float3 q = boundary_state_rare(kind, bv, d.z[k], L, n1, n2, P.g);
                 hre = q.x;
                 uhr = q.y;
                 vhr = q.z;
@@ -1759,7 +1766,7 @@ agx_status agx_pool_set_boundary(agx_pool p, int32_t sid, const int32_t* kind, c
   if (B == 0) return AGX_OK;
   bool rare = false;
   for (int64_t i = 0; i < B; i++) {
-    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_CHARACTERISTIC)
+    if (kind[i] < AGX_BC_NONE || kind[i] > AGX_BC_INFLOW)
       return pfail(AGX_E_INVALID, "bad boundary kind %d at %lld", kind[i], (long long)i);
     rare |= kind[i] >= AGX_BC_TRANSMISSIVE_SET_STAGE;
   }

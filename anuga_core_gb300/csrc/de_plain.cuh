@@ -92,6 +92,7 @@ enum BoundaryKind : int {
   BK_TRANSMISSIVE_ZERO_MOM = 8,   // stage of the edge, momenta zero
   BK_FLATHER = 9,                 // outside stage given, zero outside velocity (characteristics)
   BK_CHARACTERISTIC = 10,         // stage given, momentum of a simple incoming wave (Riemann invariant)
+  BK_INFLOW = 11,                 // stage = edge bed + a depth, momenta given
 };
 
 // ---- per-cell meta bits (conn.w) -----------------------------------------
@@ -652,6 +653,9 @@ AGX_HD void boundary_value(int kind, double n1, double n2, double we, double uhe
       break;
     case BK_TRANSMISSIVE_ZERO_MOM:    // boundaries.py:520-552
       wb = we; uhb = 0.0; vhb = 0.0;
+      break;
+    case BK_INFLOW:                   // boundaries.py:902-992 (depth 1 above the edge bed)
+      wb = ze + val[0]; uhb = val[1]; vhb = val[2];
       break;
     case BK_CHARACTERISTIC: {         // boundaries.py:757-848 (the vectorised form)
       const double wo = val[0];

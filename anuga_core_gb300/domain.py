@@ -492,7 +492,7 @@ class Domain:
                 s = 3 * np.asarray(m.boundary_cells)[ids] + np.asarray(m.boundary_edges)[ids]
                 nrm = np.asarray(m.normals).reshape(-1, 2)
                 mid = np.asarray(m.edge_midpoint_coordinates)
-                vals[ids] = B.edge_values(t, nrm[s, 0], nrm[s, 1], mid[s, 0], mid[s, 1])
+                vals[ids] = B.edge_values(t, nrm[s, 0], nrm[s, 1], mid[s, 0], mid[s, 1], tag)
             elif k in (_lib.BC_DIRICHLET, _lib.BC_TRANSMISSIVE_N0, _lib.BC_TRANSMISSIVE_SET_STAGE, _lib.BC_FLATHER,
                        _lib.BC_CHARACTERISTIC):
                 vals[ids] = B.values(t)

@@ -100,6 +100,7 @@ enum {
 #define AGX_BC_TRANSMISSIVE_ZERO_MOM  8  /* stage of the edge, momenta zero (boundaries.py:520-552) */
 #define AGX_BC_FLATHER         9  /* outside stage given, zero outside velocity (boundaries.py:1096-1330) */
 #define AGX_BC_CHARACTERISTIC 10  /* stage given, incoming-wave momentum (boundaries.py:639-848) */
+#define AGX_BC_INFLOW         11  /* stage = edge bed + value 0 (a depth), momenta given (boundaries.py:902-992) */
 
 /* Per-step statistics returned by agx_advance (generic_domain.py:1200
  * timestepping_statistics and the evolve bookkeeping). */

@@ -398,6 +398,15 @@ class OracleDomain:
             self.stage_b[ids] = np.where(dry, q0_dry, q0_wet)
             self.xmom_b[ids] = np.where(dry, 0.0 * q1, q1_wet)
             self.ymom_b[ids] = np.where(dry, 0.0 * q2, q2_wet)
+        elif kind == "inflow":                    # boundaries.py:902-992 (slope 0: depth 1)
+            rate = float(vals)
+            length = 0.0
+            for j in range(len(ids)):
+                length += self.edgelengths[s[j]]
+            mu = rate / length
+            self.stage_b[ids] = self.bed_e[s] + 1.0
+            self.xmom_b[ids] = mu * (-n1)
+            self.ymom_b[ids] = mu * (-n2)
         elif kind == "time_space":                # generic_boundary_conditions.py:419-517
             t = self.starttime + self.relative_time
             x = self.edge_coordinates[2 * s]

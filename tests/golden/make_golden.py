@@ -283,7 +283,16 @@ def build_time_space_channel(m=16, n=8, L=160.0, W=80.0):
     return d, extra
 
 
+def build_inflow_channel(m=16, n=8, L=160.0, W=80.0):
+    d, extra = build_open_channel(m, n, L, W)
+    from anuga.shallow_water.boundaries import Inflow_boundary
+    d.set_boundary({"left": Inflow_boundary(d, rate=2.0), "right": anuga.Transmissive_boundary(d),
+                    "top": anuga.Reflective_boundary(d), "bottom": anuga.Reflective_boundary(d)})
+    return d, extra
+
+
 def boundary_fixtures():
+    trajectory_fixture("traj_channel_inflow_de1.npz", build_inflow_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_time_space_de1.npz", build_time_space_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_characteristic_de1.npz", build_characteristic_channel, "DE1", 2.0, 12.0)
     trajectory_fixture("traj_channel_boundaries_de1.npz", build_open_channel, "DE1", 2.0, 12.0)

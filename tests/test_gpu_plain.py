@@ -432,6 +432,24 @@ def test_time_space_boundary_matches_reference(golden):
         assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_inflow_boundary_matches_reference(golden, precision):
+    f = golden("traj_channel_inflow_de1.npz")
+    d = _channel_domain(f, "DE1", precision=precision)
+    d.set_boundary({"left": agx.Inflow_boundary(d, rate=2.0), "right": agx.Transmissive_boundary(d),
+                    "top": agx.Reflective_boundary(d), "bottom": agx.Compute_fluxes_boundary()})
+    d.set_boundary({"bottom": agx.Reflective_boundary(d)})
+    z = f["init.elevation_c"]
+    for i, t in enumerate(d.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))):
+        Q = d.quantities
+        if precision == "fp64":
+            assert normwise(Q["stage"].centroid_values, f["stage"][i]) <= STATE_TOL, i
+            assert normwise(Q["xmomentum"].centroid_values, f["xmom"][i]) <= 1e-10, i
+        else:
+            err = np.abs(np.maximum(Q["stage"].centroid_values - z, 0) - np.maximum(f["stage"][i] - z, 0)).max()
+            assert err <= 1.0e-3, (i, err)
+
+
 def test_time_stage_zero_momentum_matches_oracle(oracle_mod, golden):
     f = golden("traj_channel_boundaries_de1.npz")
     fn = lambda t: 0.6 + 0.05 * np.sin(0.2 * t)

@@ -212,3 +212,21 @@ def test_oracle_time_space_boundary_bit_exact(golden, oracle_mod):
     for i, r in enumerate(res):
         assert np.array_equal(r[1], f["stage"][i]), i
         assert np.array_equal(r[2], f["xmom"][i]), i
+
+
+def test_oracle_inflow_boundary_bit_exact(golden, oracle_mod):
+    """Inflow_boundary (shallow_water/boundaries.py:902-992)."""
+    f = golden("traj_channel_inflow_de1.npz")
+    p, e, b = rectangular_cross(int(f["mesh.m"]), int(f["mesh.n"]), 160.0, 80.0)
+    M = Mesh(p, e, b)
+    od = oracle_mod.OracleDomain(M, "DE1")
+    od.set_centroid_state(f["init.stage"], f["init.xmom"], f["init.ymom"], f["init.elevation_c"], f["init.friction"])
+    od.set_bed_vertex_values(f["init.elevation_v"])
+    kinds = {"left": ("inflow", 2.0), "right": ("transmissive", None), "top": R, "bottom": R}
+    od.set_boundaries([(M.tag_boundary_cells[t], kinds[t][0], kinds[t][1]) for t in M.tag_boundary_cells])
+    res = [(od.number_of_steps, od.stage_c.copy(), od.xmom_c.copy())
+           for t in od.evolve(yieldstep=float(f["yieldstep"]), finaltime=float(f["finaltime"]))]
+    assert [r[0] for r in res] == list(f["steps"])
+    for i, r in enumerate(res):
+        assert np.array_equal(r[1], f["stage"][i]), i
+        assert np.array_equal(r[2], f["xmom"][i]), i
