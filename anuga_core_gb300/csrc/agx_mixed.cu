@@ -477,13 +477,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
     __syncthreads();
     float ew = 0.f, ex = 0.f, ey = 0.f, smax = 0.f, bfl = 0.f;
     float4 g3 = make_float4(0.f, 0.f, 0.f, 0.f), g4 = g3;
-    // the FP64 state of the fused update is loaded before the flux loop
     double sw = 0.0, suh = 0.0, svh = 0.0;
-    if (FUSED2 && valid) {
-      sw = d.wB[k];
-      suh = d.uhB[k];
-      svh = d.vhB[k];
-    }
     if (valid) {
       const float4 g2 = d.g2[k];
       g3 = d.g3[k];
@@ -635,6 +629,9 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
       int neg = 0;
       double added = 0.0;
       if (valid) {
+        sw = d.wB[k];
+        suh = d.uhB[k];
+        svh = d.vhB[k];
         double h = sw, uh = suh, vh = svh;
         neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
                           S->clock.timestep32, added);
