@@ -1000,6 +1000,10 @@ struct Pool {
   std::vector<int> bnd_owner;    // host: boundary slot owner (-1 free)
   std::vector<ScnHost> scn;
   PoolScn* scn_host = nullptr;   // pinned mirror of d.scn
+  // scn_host equals d.scn: set by every pull and push, cleared by every
+  // launch of a kernel that writes the headers (the step kernels, operators
+  // and protect-in-place); a pull that may be skipped then costs nothing.
+  bool scn_fresh = false;
   double* staging = nullptr;     // device [cap_cells * 3] for permuted copies
   double* staging_host = nullptr;
   cudaStream_t stream = nullptr, own_stream = nullptr;
@@ -1087,13 +1091,23 @@ static agx_status psync(Pool* p) {
   PCK(cudaStreamSynchronize(p->stream));
   return AGX_OK;
 }
-static agx_status pull_scn(Pool* p) {
+// Header exchange.  `may_skip`: callers that only read the headers, or
+// change them and push them straight back, take the host mirror when no
+// header-writing kernel has run since the last exchange.
+static agx_status pull_scn(Pool* p, bool may_skip = false) {
+  if (may_skip && p->scn_fresh) return AGX_OK;
+  p->scn_fresh = false;
   PCK(cudaMemcpyAsync(p->scn_host, p->d.scn, sizeof(PoolScn) * p->cap_scn, cudaMemcpyDeviceToHost, p->stream));
-  return psync(p);
+  agx_status st = psync(p);
+  p->scn_fresh = st == AGX_OK;
+  return st;
 }
 static agx_status push_scn(Pool* p) {
+  p->scn_fresh = false;
   PCK(cudaMemcpyAsync(p->d.scn, p->scn_host, sizeof(PoolScn) * p->cap_scn, cudaMemcpyHostToDevice, p->stream));
-  return psync(p);
+  agx_status st = psync(p);
+  p->scn_fresh = st == AGX_OK;
+  return st;
 }
 
 static MParams make_mparams(const agx_params& a) {
@@ -1140,6 +1154,7 @@ static int nblk1(int n) { return (n + 255) / 256; }
 // second RK2 stage, the operators of the step loop and the clocks.
 static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   const PoolDev& d = p->d;
+  p->scn_fresh = false;
   const int S = p->cap_scn;
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
@@ -1164,6 +1179,7 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
 // Flux kernel of stage 2 or 3 (stage 3 only when some scenario has three).
 static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
   const PoolDev& d = p->d;
+  p->scn_fresh = false;
   const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
   if (stage == 3 && !p->rk3_any) return cudaSuccess;
   if (stage == 2) {
@@ -1189,6 +1205,7 @@ static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
 // The operators of the step loop and the clocks.
 static cudaError_t enqueue_step_end(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
   const PoolDev& d = p->d;
+  p->scn_fresh = false;
   const int S = p->cap_scn;
   for (size_t s = 0; s < p->scn.size(); s++) {
     const ScnHost& sh = p->scn[s];
@@ -1543,11 +1560,11 @@ agx_status agx_pool_remove(agx_pool p, int32_t sid) {
 static agx_status ensure_work(Pool* p, int sid) {
   ScnHost& sh = p->scn[sid];
   if (!sh.work_dirty) return AGX_OK;
-  k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 0, sid);
+  k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 0, sid);   // writes the work records only
   count_launch();
   PCK(cudaGetLastError());
   sh.work_dirty = false;
-  return psync(p);
+  return AGX_OK;
 }
 
 // Field access in the caller's (original) cell order.
@@ -1620,15 +1637,21 @@ static bool host_mapped(const void* ptr) {
 }
 
 // Direct exchange with mapped host buffers, walked in the caller's order
-// (contiguous on the host side; permuted on the device side).
-__global__ void k_state_from_host(double* w, double* uh, double* vh, const double* z, const double* hw,
-                                  const double* huh, const double* hvh, const int* inv, int n) {
+// (contiguous on the host side; permuted on the device side).  The read also
+// writes each cell's work record (the k_pool_prep pass without in-place
+// protection), so the next step needs no separate pass over the state.
+__global__ void k_state_from_host(double* w, double* uh, double* vh, const double* z, float4* W0,
+                                  const double* area, const PoolScn* S, const double* hw, const double* huh,
+                                  const double* hvh, const int* inv, int n) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o < n) {
     const int j = inv[o];
-    w[j] = hw[o] - z[j];
-    uh[j] = huh[o];
-    vh[j] = hvh[o];
+    double h = hw[o] - z[j], u = huh[o], v = hvh[o];
+    w[j] = h;
+    uh[j] = u;
+    vh[j] = v;
+    double added;
+    W0[j] = protect_prep(S->P, h, u, v, area[j], added);
   }
 }
 __global__ void k_state_to_host(double* hw, double* huh, double* hvh, const double* w, const double* uh,
@@ -1655,11 +1678,12 @@ agx_status agx_pool_set_state(agx_pool p, int32_t sid, const double* w, const do
   const int c0 = sh.tile0 * TILE;
   cudaStream_t st = p->stream;
   if (host_mapped(w) && host_mapped(uh) && host_mapped(vh)) {
-    k_state_from_host<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->d.z + c0, w, uh,
-                                                    vh, sh.inv, (int)n);
+    k_state_from_host<<<nblk1((int)n), 256, 0, st>>>(p->d.wA + c0, p->d.uhA + c0, p->d.vhA + c0, p->d.z + c0,
+                                                    p->d.W0 + c0, p->d.area + c0, p->d.scn + sid, w, uh, vh,
+                                                    sh.inv, (int)n);
     count_launch();
     PCK(cudaGetLastError());
-    sh.work_dirty = true;
+    sh.work_dirty = false;
     return psync(p);
   }
   PCK(cudaMemcpyAsync(p->staging, w, n * 8, cudaMemcpyHostToDevice, st));
@@ -1956,6 +1980,7 @@ agx_status agx_pool_apply_operator(agx_pool p, int32_t sid, int32_t op, double r
   if (st) return st;
   PoolOp o = sh.ops[op];
   o.dt = timestep;
+  p->scn_fresh = false;
   if (o.n > 0) {
     if (o.kind == 1) {
       k_pool_inlet<<<1, INLET_TPB, 0, p->stream>>>(p->d, o, op, rate, factor, 1);
@@ -1984,6 +2009,7 @@ agx_status agx_pool_clear_operators(agx_pool p, int32_t sid) {
 // surrounded-dry zeroing, fresh work record).
 agx_status agx_pool_distribute(agx_pool p, int32_t sid) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  p->scn_fresh = false;
   k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 1, sid);
   k_pool_sdry<<<p->grid, TILE, 0, p->stream>>>(p->d, sid);
   k_pool_prep<<<p->grid, TILE, 0, p->stream>>>(p->d, 0, sid);
@@ -1996,7 +2022,7 @@ agx_status agx_pool_distribute(agx_pool p, int32_t sid) {
 agx_status agx_pool_set_clock(agx_pool p, int32_t sid, double time, double yield_time, double final_time,
                               int64_t max_steps) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
-  agx_status st = pull_scn(p);
+  agx_status st = pull_scn(p, true);
   if (st) return st;
   Clock& c = p->scn_host[sid].clock;
   c.time = time;
@@ -2014,7 +2040,7 @@ agx_status agx_pool_set_clock(agx_pool p, int32_t sid, double time, double yield
 
 agx_status agx_pool_deactivate(agx_pool p, int32_t sid) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
-  agx_status st = pull_scn(p);
+  agx_status st = pull_scn(p, true);
   if (st) return st;
   p->scn_host[sid].active = 0;
   return push_scn(p);
@@ -2042,12 +2068,13 @@ agx_status agx_pool_advance(agx_pool p, int32_t* n_done) {
   if (!p) return pfail(AGX_E_INVALID, "null pool");
   for (int s = 0; s < p->cap_scn; s++)
     if (p->scn[s].alive) { agx_status st = ensure_work(p, s); if (st) return st; }
-  agx_status st = pull_scn(p);
+  agx_status st = pull_scn(p, true);
   if (st) return st;
   int nact = 0;
   for (int s = 0; s < p->cap_scn; s++) if (p->scn_host[s].alive && p->scn_host[s].active) nact++;
   if (nact == 0) { if (n_done) *n_done = 0; return AGX_OK; }
   if (!p->graph_valid && (st = pool_build_graph(p)) != AGX_OK) return st;
+  p->scn_fresh = false;
   PCK(cudaGraphLaunch(p->exec, p->stream));
   if ((st = pull_scn(p))) return st;
   long long iters = 0;
@@ -2102,7 +2129,7 @@ agx_status agx_pool_step_end(agx_pool p, int32_t* n_done) {
 
 agx_status agx_pool_get_stats(agx_pool p, int32_t sid, agx_step_stats* out) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !out) return pfail(AGX_E_INVALID, "bad scenario");
-  agx_status st = pull_scn(p);
+  agx_status st = pull_scn(p, true);
   if (st) return st;
   fill_stats_p(&p->scn_host[sid].clock, out);
   const int e = p->scn_host[sid].clock.error;
@@ -2117,7 +2144,7 @@ agx_status agx_pool_get_stats(agx_pool p, int32_t sid, agx_step_stats* out) {
 agx_status agx_pool_operator_influx(agx_pool p, int32_t sid, int32_t op, double* v) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || op < 0 || op >= MAX_OPS || !v)
     return pfail(AGX_E_INVALID, "bad arguments");
-  agx_status st = pull_scn(p);
+  agx_status st = pull_scn(p, true);
   if (st) return st;
   *v = p->scn_host[sid].clock.op_influx[op];
   return AGX_OK;
@@ -2188,6 +2215,7 @@ agx_status agx_pool_launch_chunk(agx_pool p, int64_t max_steps) {
   if ((st = push_scn(p))) return st;
   if (nact == 0) return AGX_OK;
   if (!p->graph_valid && (st = pool_build_graph(p)) != AGX_OK) return st;
+  p->scn_fresh = false;
   PCK(cudaGraphLaunch(p->exec, p->stream));
   return AGX_OK;
 }
