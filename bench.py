@@ -399,9 +399,9 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # category's launches of one step, divided by the cells of the captured mesh).
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
-        "bytes_per_cell": (117.630976e6 + 11.483136e6 + 169.704960e6 + 24.624896e6) / 1.0e6,
+        "bytes_per_cell": (117.617408e6 + 10.710272e6 + 169.683968e6 + 23.024640e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
-                "(m=500, MINB=6 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
+                "(m=500, MINB=8 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
                 "scaled by cells; profiles/k_pool_flux_inflow_bumps_1M_mixed.md"},
     ("fp64", "extrap"): {
         "bytes_per_cell": 2 * (125.701632e6 + 78.489088e6) / 1.0e6,
