@@ -1,0 +1,97 @@
+"""Edge cases of the mixed-precision pool: a one-triangle mesh (three
+boundary edges, a tile holding one cell and 127 unused slots), a completely
+dry domain, and meshes whose last tile is partly filled (4, 124, 128 and 132
+triangles against 128-cell tiles).
+
+Bars: depths within 1 mm of the plain FP64 form on the same inputs; a dry
+domain keeps its stage bitwise and takes one step of the maximum timestep
+to reach the yield time, as the plain form does.
+"""
+import numpy as np
+import pytest
+
+from anuga_core_gb300.mesh import Mesh, rectangular_cross
+from helpers import make_domain, random_state
+
+pytestmark = pytest.mark.gpu
+
+DEPTH_TOL = 1.0e-3   # metres
+
+
+def _depth(d):
+    z = d.quantities["elevation"].centroid_values
+    return np.maximum(d.quantities["stage"].centroid_values - z, 0.0)
+
+
+def test_single_triangle_within_1mm_of_plain():
+    p = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]])
+    e = np.array([[0, 1, 2]])
+    st = dict(elevation=np.zeros(1), stage=np.full(1, 0.5), xmom=np.full(1, 0.1), ymom=np.zeros(1),
+              friction=np.zeros(1))
+    kinds = {"exterior": ("reflective", None)}
+    res = {}
+    for precision in ("fp64", "mixed"):
+        d = make_domain(p, e, None, "DE0", st, kinds, precision=precision)
+        for _ in d.evolve(yieldstep=0.1, finaltime=0.3):
+            pass
+        assert abs(d.get_time() - 0.3) < 1e-12
+        res[precision] = _depth(d)
+    assert np.abs(res["mixed"] - res["fp64"]).max() <= DEPTH_TOL
+
+
+def test_dry_domain_keeps_its_stage():
+    p, e, b = rectangular_cross(5, 5, 10.0, 10.0)
+    mesh = Mesh(p, e, b)
+    z = mesh.centroid_coordinates[:, 0] * 0.1
+    st = dict(elevation=z, stage=z.copy(), xmom=np.zeros_like(z), ymom=np.zeros_like(z), friction=np.zeros_like(z))
+    d = make_domain(p, e, b, "DE1", st, {t: ("reflective", None) for t in mesh.tag_boundary_cells},
+                    precision="mixed")
+    for _ in d.evolve(yieldstep=5.0, finaltime=5.0):
+        pass
+    assert np.array_equal(d.quantities["stage"].centroid_values, z)
+    assert d.total_steps == 1
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (31, 1), (8, 4), (11, 3)])
+def test_partly_filled_last_tile_within_1mm_of_plain(m, n):
+    p, e, b = rectangular_cross(m, n, 4.0 * m, 4.0 * n)
+    mesh = Mesh(p, e, b)
+    assert len(mesh) == 4 * m * n
+    st = random_state(mesh, seed=100 + m + n, dry_fraction=0.3)
+    kinds = {t: ("reflective", None) for t in mesh.tag_boundary_cells}
+    res = {}
+    for precision in ("fp64", "mixed"):
+        d = make_domain(p, e, b, "DE1", st, kinds, precision=precision)
+        for _ in d.evolve(yieldstep=0.5, finaltime=2.0):
+            pass
+        res[precision] = (_depth(d), d.quantities["stage"].centroid_values.sum())
+    assert np.abs(res["mixed"][0] - res["fp64"][0]).max() <= DEPTH_TOL
+
+
+def test_pool_rejects_a_scenario_beyond_its_capacity():
+    """A scenario larger than the free cells is refused with an error; the
+    pool keeps working for scenarios that fit."""
+    from anuga_core_gb300 import _lib, mixed
+    from anuga_core_gb300.serve import de1_params
+    pool = mixed.Pool(256, 4096, 2)
+    try:
+        free = pool.capacity()["cells"]
+        big = Mesh(*rectangular_cross(16, 16, 16.0, 16.0))          # 1024 triangles
+        assert len(big) > free
+        with pytest.raises(_lib.AgxError):
+            pool.add(big, de1_params())
+        assert pool.capacity()["cells"] == free
+        small = Mesh(*rectangular_cross(2, 2, 2.0, 2.0))           # 16 triangles
+        sid = pool.add(small, de1_params())
+        z = np.zeros(len(small))
+        pool.set_field(sid, "elev_c", z)
+        pool.set_field(sid, "stage_c", z + 0.5)
+        nb = small.boundary_length
+        pool.set_boundary(sid, np.full(nb, _lib.BC_REFLECTIVE, np.int32), np.zeros((nb, 3)))
+        pool.distribute(sid)
+        pool.set_clock(sid, 0.0, 1e300, 1.0, 0)
+        assert pool.advance() == 1                                  # one launch runs to the final time
+        assert abs(pool.stats(sid).time - 1.0) < 1e-12
+        assert np.allclose(pool.get_field(sid, "stage_c"), 0.5)
+    finally:
+        pool.close()
