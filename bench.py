@@ -85,6 +85,9 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()            # sampling is running before the timed region starts
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
@@ -201,7 +204,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 50; 500 for --workload batch, about a second of timing)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--m", type=int, default=1000, help="mesh side (4*m*m triangles)")
@@ -215,6 +219,8 @@ def main():
                     help="inflow_bumps: one 4M-triangle mesh; batch: 256 scenarios (~20M triangles) in one pool")
     ap.add_argument("--batch-count", type=int, default=256, dest="batch_count")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 500 if args.workload == "batch" else 50
     if args.impl == "reference":
         return run_reference(args)
 
