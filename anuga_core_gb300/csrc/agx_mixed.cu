@@ -426,8 +426,6 @@ template <int STG, int MINB, bool EXT = false>
 __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   constexpr bool FUSED2 = STG >= 2;
   __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
-  __shared__ float shf[TILE / 32];
-  __shared__ double shd[TILE / 32];
   const float4* W = STG == 1 ? d.W0 : (STG == 3 ? d.W2 : d.W1);
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
     const int base = tile * TILE;
@@ -619,11 +617,17 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         d.maxs[k] = smax;
         if (smax > 0.0f) dtk = g3.w / smax;
       }
-      const float bm = block_min_f(dtk, shf);
-      const float bs = block_sum_f(bfl, shf);
-      if (threadIdx.x == 0) {      // fire-and-forget reductions (no return value)
-        if (bm < 3.0e38f) atomicMax(&S->clock.dt_key, ~(unsigned long long)__double_as_longlong((double)bm));
-        if (bs != 0.0f) atomicAdd(&S->clock.bfs_acc, (double)bs);
+      // per-warp reductions, no block barrier: the CFL minimum is order
+      // independent (the same key whatever the grouping); the boundary flux
+      // sum is accumulated by atomics in no fixed order either way
+      const float wm = warp_min_f(dtk);
+      const float ws = warp_sum_f(bfl);
+      if ((threadIdx.x & 31) == 0) {      // fire-and-forget reductions (no return value)
+        if (wm < 3.0e38f) {
+          const unsigned long long key = ~(unsigned long long)__double_as_longlong((double)wm);
+          if (key > __ldcg(&S->clock.dt_key)) atomicMax(&S->clock.dt_key, key);   // only a new maximum
+        }
+        if (ws != 0.0f) atomicAdd(&S->clock.bfs_acc, (double)ws);
       }
     } else {
       int neg = 0;
@@ -661,14 +665,16 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
           d.W0[k] = record_of(P, h, uh, vh);
         }
       }
-      const float bs = block_sum_f(bfl, shf);
-      const int anym = __syncthreads_or(__double_as_longlong(added) != 0);
-      const double ma = anym ? block_sum_d(added, shd) : 0.0;
-      const int nneg = __syncthreads_count(neg);
-      if (threadIdx.x == 0) {
-        if (bs != 0.0f) atomicAdd(&S->clock.bfs[STG == 3 ? 2 : 1], (double)bs);
-        if (ma != 0.0) atomicAdd(&S->clock.mass_added, ma);
-        if (nneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)nneg);
+      // per-warp reductions, no block barrier (the sums go to atomics in no
+      // fixed order either way)
+      const float ws = warp_sum_f(bfl);
+      const unsigned anym = __ballot_sync(0xffffffffu, __double_as_longlong(added) != 0);
+      const double wa = anym ? warp_sum_d(added) : 0.0;
+      const int wneg = __popc(__ballot_sync(0xffffffffu, neg));
+      if ((threadIdx.x & 31) == 0) {
+        if (ws != 0.0f) atomicAdd(&S->clock.bfs[STG == 3 ? 2 : 1], (double)ws);
+        if (wa != 0.0) atomicAdd(&S->clock.mass_added, wa);
+        if (wneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)wneg);
       }
     }
     __syncthreads();
