@@ -529,6 +529,22 @@ class Domain:
             op._dev_index = len(self._dev_ops)
             self._dev_ops.append(op)
 
+    def set_conserved_state(self, stage, xmomentum, ymomentum):
+        """Centroid stage, xmomentum and ymomentum in one call and one
+        device transfer (page-locked arrays are read by the device directly)."""
+        scn = self._ensure_device()
+        self._push_dirty()
+        scn.set_state(stage, xmomentum, ymomentum)
+        self._mark_device_newer(["stage_c", "xmom_c", "ymom_c"])
+
+    def get_conserved_state(self, stage=None, xmomentum=None, ymomentum=None):
+        """Centroid stage, xmomentum and ymomentum from the device in one
+        call, into the given arrays (page-locked ones are written by the
+        device directly) or new ones; returns the three arrays."""
+        scn = self._ensure_device()
+        self._push_dirty()
+        return scn.get_state(stage, xmomentum, ymomentum)
+
     def _apply_rate_now(self, op, rate, factor, dt):
         """One application of a registered Rate_operator on the device."""
         scn = self._ensure_device()

@@ -5,7 +5,10 @@ triangles against 128-cell tiles).
 
 Bars: depths within 1 mm of the plain FP64 form on the same inputs; a dry
 domain keeps its stage bitwise and takes one step of the maximum timestep
-to reach the yield time, as the plain form does.
+to reach the yield time, as the plain form does.  Also: a pool refuses a
+scenario beyond its capacity and stays usable, and the Domain's one-call
+state exchange (set_conserved_state / get_conserved_state) returns the state
+it was given on both forms, from pageable and page-locked arrays.
 """
 import numpy as np
 import pytest
@@ -95,3 +98,37 @@ def test_pool_rejects_a_scenario_beyond_its_capacity():
         assert np.allclose(pool.get_field(sid, "stage_c"), 0.5)
     finally:
         pool.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_domain_conserved_state_exchange(precision):
+    """Domain.set_conserved_state / get_conserved_state with page-locked and
+    pageable arrays: the state set is the state read back and the one the
+    quantities show; stepping continues from it."""
+    import torch
+    from anuga_core_gb300 import workloads
+    d = workloads.dam_break(m=20, flow_algorithm="DE1", precision=precision)
+    for _ in d.evolve(yieldstep=0.5, finaltime=0.5):
+        pass
+    n = len(d)
+    w0, uh0, vh0 = d.get_conserved_state()
+    assert np.array_equal(w0, d.quantities["stage"].centroid_values)
+    pin = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    z = d.quantities["elevation"].centroid_values
+    rng = np.random.default_rng(7)
+    w = z + np.maximum(w0 - z, 0.0) * (1.0 + 0.01 * rng.random(n))
+    for arrs in ([w, uh0 * 0.5, vh0 * 0.5], None):
+        if arrs is None:                                   # page-locked input
+            for dst, src in zip(pin, [w, uh0 * 0.5, vh0 * 0.5]):
+                dst[:] = src
+            arrs = pin
+        d.set_conserved_state(*arrs)
+        got = d.get_conserved_state()
+        # the mixed form keeps the depth w - z in FP64: the stage comes back as (w - z) + z
+        tol = 0.0 if precision == "fp64" else 1e-12
+        assert np.abs(got[0] - w).max() <= tol
+        assert np.array_equal(got[1], uh0 * 0.5) and np.array_equal(got[2], vh0 * 0.5)
+        assert np.abs(d.quantities["stage"].centroid_values - w).max() <= tol
+    for _ in d.evolve(yieldstep=0.5, finaltime=1.0):
+        pass
+    assert abs(d.get_time() - 1.0) < 1e-12
