@@ -380,11 +380,10 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
     barrier()
     e2.record(stream)
     w, uh, vh = pin["stage_c"], pin["xmom_c"], pin["ymom_c"]
-    for _ in range(args.steps):
-        scn.set_state(w, uh, vh)
-        scn.set_clock(d.relative_time, 1e300, -1.0)
-        scn.advance(1)
-        scn.get_state(w, uh, vh)
+    for _ in range(args.steps):              # the Domain calls a user makes
+        d.set_conserved_state(w, uh, vh)
+        d.advance_steps(1)
+        d.get_conserved_state(w, uh, vh)
     e3.record(stream)
     barrier()
     e2e_ms = max_over_ranks(e2.elapsed_time(e3), dist)
@@ -393,7 +392,8 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
            "step_roofline": step_roof, "launches": launches, "autotune": tune, "state_bytes": scn_bytes(d),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
                    "path": "conserved state w, uh, vh from and to page-locked host buffers each step through "
-                           "agx_set_state/agx_get_state (the mixed pool reads and writes mapped host memory "
+                           "Domain.set_conserved_state / advance_steps(1) / get_conserved_state (agx_set_state, "
+                           "agx_advance, agx_get_state; the mixed pool reads and writes mapped host memory "
                            "directly; the plain path copies)"}}
     del d, scn
     torch.cuda.synchronize()
