@@ -818,6 +818,7 @@ __global__ void k_pool_reset(PoolDev d, int nscn) {
   S->clock.dt_key = 0ull;
   S->clock.bfs_acc = 0.0;
   S->clock.bfs[1] = 0.0;
+  S->clock.bfs[2] = 0.0;       // third (RK3) stage's sum
 }
 
 // A fractional-step operator of one scenario: Rate_operator (kind 0) or

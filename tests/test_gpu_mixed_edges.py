@@ -132,3 +132,24 @@ def test_domain_conserved_state_exchange(precision):
     for _ in d.evolve(yieldstep=0.5, finaltime=1.0):
         pass
     assert abs(d.get_time() - 1.0) < 1e-12
+
+
+def test_rk3_boundary_flux_sums_are_per_step():
+    """The per-stage boundary flux sums reported after a step (three for
+    rk3) are that step's, on both forms: the mixed ones agree with the plain
+    FP64 ones to the FP32 flux tolerance and do not accumulate over steps."""
+    p, e, b = rectangular_cross(16, 8, 32.0, 16.0)
+    mesh = Mesh(p, e, b)
+    st = random_state(mesh, seed=21, dry_fraction=0.2)
+    kinds = {"left": ("dirichlet", (float(st["stage"].max()) + 0.3, 0.0, 0.0)), "right": ("transmissive", None),
+             "top": ("reflective", None), "bottom": ("reflective", None)}
+    res = {}
+    for precision in ("fp64", "mixed"):
+        d = make_domain(p, e, b, "DE2", st, kinds, precision=precision)
+        for _ in d.evolve(yieldstep=0.5, finaltime=2.0):
+            pass
+        assert d.total_steps > 5
+        res[precision] = np.asarray(d.boundary_flux_sum, float)[:3]
+    scale = np.abs(res["fp64"]).max()
+    assert scale > 0.0
+    assert np.abs(res["mixed"] - res["fp64"]).max() <= 1e-2 * scale, res
