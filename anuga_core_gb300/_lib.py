@@ -59,7 +59,8 @@ class StepStats(ctypes.Structure):
                 ("flux_timestep", ctypes.c_double), ("mass_added", ctypes.c_double),
                 ("boundary_flux_sum", ctypes.c_double * 3), ("steps", ctypes.c_int64),
                 ("total_steps", ctypes.c_int64), ("negative_cells", ctypes.c_int64),
-                ("reason", ctypes.c_int32), ("order", ctypes.c_int32)]
+                ("reason", ctypes.c_int32), ("order", ctypes.c_int32),
+                ("boundary_flux_integral", ctypes.c_double), ("nonfinite_cells", ctypes.c_int64)]
 
 
 class AgxError(RuntimeError):
@@ -95,6 +96,9 @@ def load(path=None):
         "agx_sww_bind": ([H, ctypes.c_int64, _i32p, _i32p], ctypes.c_int32),
         "agx_sww_frame": ([H, ctypes.c_double, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
                           ctypes.c_int32),
+        "agx_sww_frame_async": ([H, ctypes.c_double], ctypes.c_int32),
+        "agx_sww_frame_wait": ([H, P(ctypes.POINTER(ctypes.c_float)), P(ctypes.POINTER(ctypes.c_float))],
+                               ctypes.c_int32),
         "agx_get_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary": ([H, _i32p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_set_boundary_series": ([H, _f64p, ctypes.c_int64], ctypes.c_int32),
@@ -116,6 +120,7 @@ def load(path=None):
         "agx_set_riverwalls": ([H, _i32p, ctypes.c_int64, ctypes.c_int64, _f64p, _i32p, ctypes.c_int32,
                                 ctypes.c_int32, _f64p], ctypes.c_int32),
         "agx_set_clock": ([H, ctypes.c_double, ctypes.c_double, ctypes.c_double], ctypes.c_int32),
+        "agx_set_fixed_flux_timestep": ([H, ctypes.c_double], ctypes.c_int32),
         "agx_advance": ([H, ctypes.c_int64, P(StepStats)], ctypes.c_int32),
         "agx_get_stats": ([H, P(StepStats)], ctypes.c_int32),
         "agx_set_stream": ([H, ctypes.c_void_p], ctypes.c_int32),
@@ -131,6 +136,16 @@ def load(path=None):
         fn.restype = res
     _lib = L
     return L
+
+
+def _frame_arrays(fn, args, P, N):
+    """Wait through `fn` for a frame in page-locked memory and copy it out."""
+    fp = ctypes.POINTER(ctypes.c_float)
+    v, c = fp(), fp()
+    check(fn(*args, ctypes.byref(v), ctypes.byref(c)))
+    vv = np.ctypeslib.as_array(v, shape=(3 * P,)).copy().reshape(3, P) if P else np.zeros((3, 0), np.float32)
+    cc = np.ctypeslib.as_array(c, shape=(3 * N,)).copy().reshape(3, N)
+    return vv, cc
 
 
 def last_error():
@@ -252,6 +267,14 @@ class Scenario:
         check(self.L.agx_sww_frame(self.h, float(min_storable_height), v.ctypes.data_as(fp), c.ctypes.data_as(fp)))
         return v, c
 
+    def sww_frame_async(self, min_storable_height):
+        """Start forming a frame and copying it to page-locked memory; returns at once."""
+        check(self.L.agx_sww_frame_async(self.h, float(min_storable_height)))
+
+    def sww_frame_wait(self):
+        """The frame started last, as copies of (vertex [3, P], centroid [3, N]) float32."""
+        return _frame_arrays(self.L.agx_sww_frame_wait, (self.h,), self._sww_P, self.N)
+
     def device_ptr(self, name):
         p = ctypes.c_void_p()
         n = ctypes.c_int64()
@@ -351,6 +374,9 @@ class Scenario:
         st = StepStats()
         check(self.L.agx_get_stats(self.h, ctypes.byref(st)))
         return st
+
+    def set_fixed_flux_timestep(self, flux_timestep):
+        check(self.L.agx_set_fixed_flux_timestep(self.h, float(flux_timestep or 0.0)))
 
 
 def kernel_launches():

@@ -143,6 +143,7 @@ static void init_clock(Clock* c, const agx_params& p) {
   c->order = 2;
   c->default_order = 2;
   c->flux_timestep = p.evolve_max_timestep;
+  c->fluxcalls = p.timestepping_method;
 }
 
 static agx_status sync(Scenario* s) {
@@ -162,6 +163,9 @@ static agx_status push_clock(Scenario* s) {
 
 static agx_status check_errors(Scenario* s) {
   const int e = s->clock_host->error;
+  if (e & ERR_NONFINITE)
+    return fail(AGX_E_NUMERIC, "non-finite conserved quantity (NaN or Inf) in %lld cell updates; the step loop "
+                "stopped", (long long)s->clock_host->nonfinite_cells);
   if (e & ERR_NUMERIC) return fail(AGX_E_NUMERIC, "update: non-positive semi-implicit denominator");
   if (e & ERR_TIMESTEP) return fail(AGX_E_TIMESTEP, "too small timestep reached after %d steps at first order", s->prm.max_smallsteps);
   if (e & ERR_OVERSHOOT) return fail(AGX_E_OVERSHOOT, "time overshot finaltime");
@@ -327,6 +331,8 @@ agx_status agx_scenario_destroy(agx_handle h) {
   if (s->node_off) cudaFree(s->node_off);
   if (s->node_slot) cudaFree(s->node_slot);
   if (s->frame) cudaFree(s->frame);
+  if (s->frame_host) cudaFreeHost(s->frame_host);
+  if (s->frame_done) cudaEventDestroy(s->frame_done);
   if (s->bseries) cudaFree(s->bseries);
   if (s->rw_mem) cudaFree(s->rw_mem);
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -391,12 +397,18 @@ agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, co
   if (h->node_off) cudaFree(h->node_off);
   if (h->node_slot) cudaFree(h->node_slot);
   if (h->frame) cudaFree(h->frame);
+  if (h->frame_host) cudaFreeHost(h->frame_host);
+  if (h->frame_done) cudaEventDestroy(h->frame_done);
   h->node_off = h->node_slot = nullptr;
-  h->frame = nullptr;
+  h->frame = h->frame_host = nullptr;
+  h->frame_done = nullptr;
   h->P = (int)P;
+  const size_t fbytes = ((size_t)3 * P + 3 * (size_t)h->N) * 4 + 4;
   CK(cudaMalloc(&h->node_off, (size_t)(P + 1) * 4));
   CK(cudaMalloc(&h->node_slot, (size_t)3 * h->N * 4 + 4));
-  CK(cudaMalloc(&h->frame, ((size_t)3 * P + 3 * (size_t)h->N) * 4 + 4));
+  CK(cudaMalloc(&h->frame, fbytes));
+  CK(cudaMallocHost(&h->frame_host, fbytes));
+  CK(cudaEventCreateWithFlags(&h->frame_done, cudaEventDisableTiming));
   CK(cudaMemcpyAsync(h->node_off, node_offsets, (size_t)(P + 1) * 4, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->node_slot, node_slots, (size_t)3 * h->N * 4, cudaMemcpyHostToDevice, h->stream));
   return sync(h);
@@ -410,6 +422,26 @@ agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex
   if (h->P > 0) CK(cudaMemcpyAsync(vertex_out, h->frame, (size_t)3 * h->P * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(centroid_out, h->frame + 3 * (size_t)h->P, (size_t)3 * h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   return sync(h);
+}
+
+agx_status agx_sww_frame_async(agx_handle h, double min_storable_height) {
+  AGX_TRACE("agx_sww_frame_async");
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
+  CK(enqueue_sww_frame(h, h->stream, min_storable_height));
+  CK(cudaMemcpyAsync(h->frame_host, h->frame, ((size_t)3 * h->P + 3 * (size_t)h->N) * 4, cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaEventRecord(h->frame_done, h->stream));
+  return AGX_OK;
+}
+
+agx_status agx_sww_frame_wait(agx_handle h, const float** vertex, const float** centroid) {
+  if (!h || !vertex || !centroid) return fail(AGX_E_INVALID, "bad arguments");
+  if (!h->frame_host) return fail(AGX_E_STATE, "agx_sww_bind first");
+  CK(cudaEventSynchronize(h->frame_done));
+  *vertex = h->frame_host;
+  *centroid = h->frame_host + 3 * (size_t)h->P;
+  return AGX_OK;
 }
 
 agx_status agx_device_ptr(agx_handle h, int32_t f, void** ptr, int64_t* n) {
@@ -653,6 +685,15 @@ agx_status agx_divide_conserved(agx_handle h, double divisor) {
   return sync(h);
 }
 
+agx_status agx_set_fixed_flux_timestep(agx_handle h, double flux_timestep) {
+  if (!h) return fail(AGX_E_INVALID, "null handle");
+  if (!(flux_timestep >= 0.0)) return fail(AGX_E_INVALID, "flux_timestep needs to be greater than 0.0");
+  agx_status st = pull_clock(h);
+  if (st) return st;
+  h->clock_host->fixed_flux_dt = flux_timestep;
+  return push_clock(h);
+}
+
 agx_status agx_set_clock(agx_handle h, double time, double yield_time, double final_time) {
   if (!h) return fail(AGX_E_INVALID, "null handle");
   agx_status st = pull_clock(h);
@@ -677,6 +718,8 @@ static void fill_stats(const Clock* c, agx_step_stats* o) {
   o->negative_cells = c->negative_cells;
   o->reason = c->reason;
   o->order = c->order;
+  o->boundary_flux_integral = c->bf_integral;
+  o->nonfinite_cells = c->nonfinite_cells;
 }
 
 agx_status agx_set_stream(agx_handle h, void* stream) {

@@ -25,12 +25,24 @@ struct Clock {
   double bfs_acc;
   unsigned long long dt_key;             // ~bits(dt) of the running minimum (0 = none)
   long long steps_call, total_steps, steps_target, negative_cells;
+  long long nonfinite_cells;             // cell updates that produced a NaN or an infinity
   int smallsteps, max_smallsteps, order, default_order;
-  int error, reason, pad0, pad1;
+  int error, reason, fluxcalls, pad1;    // fluxcalls: stages per step (1 euler, 2 rk2, 3 rk3)
+  double bf_integral;                    // time integral of the boundary flux sums
+  double fixed_flux_dt;                  // > 0: set_fixed_flux_timestep (replaces the CFL minimum)
   double op_influx[MAX_OPS];
 };
 
-enum ErrorBits { ERR_NUMERIC = 1, ERR_TIMESTEP = 2, ERR_OVERSHOOT = 4, ERR_NAN = 8, ERR_STEPCAP = 16 };
+enum ErrorBits { ERR_NUMERIC = 1, ERR_TIMESTEP = 2, ERR_OVERSHOOT = 4, ERR_NAN = 8, ERR_STEPCAP = 16,
+                 ERR_NONFINITE = 32 };
+
+// A double that is NaN or an infinity (biased exponent all ones), tested on
+// the high word with integer operations.
+__host__ __device__ inline bool nonfinite64(double x) {
+  long long b;
+  memcpy(&b, &x, 8);
+  return ((b >> 52) & 0x7ff) == 0x7ff;
+}
 // hard cap on the steps one agx_advance call may take on the device
 constexpr long long MAX_STEPS_PER_CALL = 20000000;
 
@@ -46,6 +58,7 @@ __host__ __device__ inline void timestep_logic(Clock* c) {
     memcpy(&v, &bits, 8);
     flux_dt = v;
   }
+  if (c->fixed_flux_dt > 0.0) flux_dt = c->fixed_flux_dt;     // generic_domain.py:2358-2359
   c->flux_timestep = flux_dt;
   double ts = fmin(c->cfl * flux_dt, c->max_dt);
   c->recorded_max = fmax(ts, c->recorded_max);
@@ -76,6 +89,16 @@ __host__ __device__ inline void timestep_logic(Clock* c) {
 // Guards keep the device loop finite: a NaN time or timestep, a non-positive
 // timestep or the per-call step cap end it with an error.
 __host__ __device__ inline int clock_logic(Clock* c) {
+  // boundary_flux_integral_operator.__call__ (operators/boundary_flux_integral_operator.py:44-62),
+  // which the reference's Domain applies after every step: the step's
+  // boundary flux sums weighted by its stages
+  if (c->fluxcalls == 1) {
+    c->bf_integral = c->bf_integral + c->timestep * c->bfs[0];
+  } else if (c->fluxcalls == 2) {
+    c->bf_integral = c->bf_integral + 0.5 * c->timestep * (c->bfs[0] + c->bfs[1]);
+  } else if (c->fluxcalls == 3) {
+    c->bf_integral = c->bf_integral + 1.0 / 6.0 * c->timestep * (c->bfs[0] + c->bfs[1] + 4.0 * c->bfs[2]);
+  }
   c->time = c->time + c->timestep;
   c->steps_call += 1;
   c->total_steps += 1;
@@ -164,6 +187,8 @@ struct Scenario {
   int* node_off = nullptr;
   int* node_slot = nullptr;
   float* frame = nullptr;
+  float* frame_host = nullptr;           // pinned copy of the last frame (asynchronous output)
+  cudaEvent_t frame_done = nullptr;      // recorded after that copy
   agx_params prm{};
   Dev d{};
   void* arena = nullptr;

@@ -68,6 +68,7 @@ struct PoolDev {
   float4* g4;                // dz0 dz1 dz2 inv_area
   double *wA, *uhA, *vhA, *wB, *uhB, *vhB, *z;
   const double* area;
+  const double* radius;      // FP64 radius of each cell (the CFL quotient of the selected cell)
   float* eta;
   float4 *W0, *W1;           // work records (h, u, v, -) of stage 1 / stage 2
   float4* W2;                // of the third RK3 stage (allocated with the first rk3 scenario)
@@ -88,6 +89,11 @@ __device__ __forceinline__ int nedge_of(int meta, int i) { return (meta >> (2 * 
 
 __device__ __forceinline__ float warp_min_f(float x) {
   for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_down_sync(0xffffffffu, x, o));
+  return x;
+}
+// minimum over the warp, held by every lane
+__device__ __forceinline__ float warp_allmin_f(float x) {
+  for (int o = 16; o > 0; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
 }
 __device__ __forceinline__ double warp_sum_d(double x) {
@@ -276,11 +282,14 @@ __device__ __forceinline__ float4 record_of(const MParams& P, double depth, doub
 // protect + preparation zeroing (distribute_to_vertices_and_edges), the
 // surrounded-by-dry zeroing, Manning friction with its semi-implicit factor
 // (sw_domain_openmp.c:1954-1986, quantity.c:772-818) and fix_negative_cells.
-// The increments dt*E (and the friction correction) are formed in FP32 and
-// accumulated into the FP64 state with one FP64 add per quantity.
+// The explicit increments dt*E use the FP64 timestep of the clock (one FP64
+// fused multiply-add per quantity, so the volume applied is the one the
+// clock's time advance implies); the friction factor and its correction
+// x (q + dt E) are formed in FP32 and subtracted in FP64.
 // Returns 1 if the cell was fixed as negative; depth1 = w - z afterwards.
 __device__ __forceinline__ int update_lean(const MParams& P, double& depth, double& uh, double& vh,
-                                           const double* area, float eta, float4 Ek, float dt32, double& added) {
+                                           const double* area, float eta, float4 Ek, double dt, float dt32,
+                                           double& added) {
   const float h = d2f_bits(depth);
   added = 0.0;
   if (h <= P.hmin) {
@@ -294,14 +303,13 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& depth, doub
   if (Ek.w != 0.0f) { uh = 0.0; vh = 0.0; }
   const float uh32 = d2f_bits(uh), vh32 = d2f_bits(vh);
   const float x = manning_x(P, fmaxf(h, 0.0f), uh32, vh32, eta, dt32);
-  const float dw = dt32 * Ek.x;
-  float du = dt32 * Ek.y;
-  float dv = dt32 * Ek.z;
-  du = du - x * (uh32 + du);
-  dv = dv - x * (vh32 + dv);
-  depth = depth + f2d_bits(dw);
-  uh = uh + f2d_bits(du);
-  vh = vh + f2d_bits(dv);
+  depth = fma(dt, f2d_bits(Ek.x), depth);
+  uh = fma(dt, f2d_bits(Ek.y), uh);
+  vh = fma(dt, f2d_bits(Ek.z), vh);
+  if (x != 0.0f) {
+    uh = uh - f2d_bits(x * (uh32 + dt32 * Ek.y));
+    vh = vh - f2d_bits(x * (vh32 + dt32 * Ek.z));
+  }
   if (negative_bits(depth)) {
     depth = 0.0;
     uh = 0.0;
@@ -309,6 +317,14 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& depth, doub
     return 1;
   }
   return 0;
+}
+
+// A NaN or an infinity in a scenario's conserved state: counted, and the
+// scenario's clock stops its step loop with an error (the CFL minimum would
+// otherwise pass over the cell and let the NaN spread).
+__device__ __noinline__ void report_nonfinite(PoolScn* S, int n) {
+  atomicAdd((unsigned long long*)&S->clock.nonfinite_cells, (unsigned long long)n);
+  atomicOr(&S->clock.error, (int)ERR_NONFINITE);
 }
 
 __device__ __forceinline__ float warp_sum_f(float x) {
@@ -617,20 +633,24 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         d.maxs[k] = smax;
         if (smax > 0.0f) dtk = g3.w / smax;
       }
-      // per-warp reductions, no block barrier: the CFL minimum is order
-      // independent (the same key whatever the grouping); the boundary flux
-      // sum is accumulated by atomics in no fixed order either way
-      const float wm = warp_min_f(dtk);
+      // per-warp reductions, no block barrier.  The CFL key selects the
+      // cell of the smallest FP32 radius/speed (ties: the higher index) and
+      // is order independent whatever the grouping; the timestep kernel
+      // forms that cell's quotient in FP64.  The boundary flux sum is
+      // accumulated by atomics in no fixed order either way.
+      const float wm = warp_allmin_f(dtk);
       const float ws = warp_sum_f(bfl);
+      const unsigned win = __ballot_sync(0xffffffffu, dtk == wm);
       if ((threadIdx.x & 31) == 0) {      // fire-and-forget reductions (no return value)
         if (wm < 3.0e38f) {
-          const unsigned long long key = ~(unsigned long long)__double_as_longlong((double)wm);
+          const int cell = k + 31 - __clz(win);
+          const unsigned long long key = ((unsigned long long)(~__float_as_uint(wm)) << 32) | (unsigned)cell;
           if (key > __ldcg(&S->clock.dt_key)) atomicMax(&S->clock.dt_key, key);   // only a new maximum
         }
         if (ws != 0.0f) atomicAdd(&S->clock.bfs_acc, (double)ws);
       }
     } else {
-      int neg = 0;
+      int neg = 0, nf = 0;
       double added = 0.0;
       if (valid) {
         sw = d.wB[k];
@@ -638,7 +658,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         svh = d.vhB[k];
         double h = sw, uh = suh, vh = svh;
         neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
-                          S->clock.timestep32, added);
+                          S->clock.timestep, S->clock.timestep32, added);
         if (STG == 2) {
           h = half_sum(h, d.wA[k]);
           uh = half_sum(uh, d.uhA[k]);
@@ -664,6 +684,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
           d.vhA[k] = vh;
           d.W0[k] = record_of(P, h, uh, vh);
         }
+        nf = nonfinite64(h) | nonfinite64(uh) | nonfinite64(vh);
       }
       // per-warp reductions, no block barrier (the sums go to atomics in no
       // fixed order either way)
@@ -671,10 +692,12 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
       const unsigned anym = __ballot_sync(0xffffffffu, __double_as_longlong(added) != 0);
       const double wa = anym ? warp_sum_d(added) : 0.0;
       const int wneg = __popc(__ballot_sync(0xffffffffu, neg));
+      const int wnf = __popc(__ballot_sync(0xffffffffu, nf));
       if ((threadIdx.x & 31) == 0) {
         if (ws != 0.0f) atomicAdd(&S->clock.bfs[STG == 3 ? 2 : 1], (double)ws);
         if (wa != 0.0) atomicAdd(&S->clock.mass_added, wa);
         if (wneg) atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)wneg);
+        if (wnf) report_nonfinite(S, wnf);
       }
     }
     __syncthreads();
@@ -699,10 +722,11 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     const MParams P = S->P;
     const int euler = !P.rk2;
     const bool valid = k < S->cell0 + S->ncell;
-    int neg = 0;
+    int neg = 0, nf = 0;
     double added = 0.0;
     if (valid) {
-      neg = update_lean(P, h, uh, vh, d.area + k, etak, Ek, S->clock.timestep32, added);
+      neg = update_lean(P, h, uh, vh, d.area + k, etak, Ek, S->clock.timestep, S->clock.timestep32, added);
+      nf = nonfinite64(h) | nonfinite64(uh) | nonfinite64(vh);
       const float4 r = record_of(P, h, uh, vh);
       if (euler) {
         d.wA[k] = h; d.uhA[k] = uh; d.vhA[k] = vh;
@@ -720,6 +744,8 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     }
     if (nb && (threadIdx.x & 31) == 0)
       atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)__popc(nb));
+    const unsigned nfb = __ballot_sync(full, nf);
+    if (nfb && (threadIdx.x & 31) == 0) report_nonfinite(S, __popc(nfb));
   }
 }
 
@@ -801,12 +827,86 @@ __global__ void k_pool_edges(PoolDev d, int sid, double* we, double* he, double*
   }
 }
 
+// One vertex slot's stage, bed and momenta in FP64 from the reconstruction of
+// its cell, formed as k_pool_edges forms the edge values and the vertex value
+// from them as the host export does (vertex i = e(i+1) + e(i+2) - e(i)).
+__device__ __forceinline__ void pool_vertex(const PoolDev& d, const MParams& P, int k, int i, double& w, double& z,
+                                            double& uh, double& vh) {
+  EdgeState es[3];
+  bool sd;
+  float4 rk;
+  reconstruct(d, P, k, d.W0, es, sd, rk);
+  const double zc = d.z[k];
+  double we[3], ze[3], ue[3], ve[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    ze[j] = zc + (double)es[j].dz;
+    we[j] = ze[j] + (double)es[j].h;
+    ue[j] = es[j].uh;
+    ve[j] = es[j].vh;
+  }
+  const int a = i == 0 ? 1 : 0, b = i == 2 ? 1 : 2;      // the two other edges, in increasing order
+  w = we[a] + we[b] - we[i];
+  z = ze[a] + ze[b] - ze[i];
+  uh = ue[a] + ue[b] - ue[i];
+  vh = ve[a] + ve[b] - ve[i];
+}
+
+// sww frame of one scenario (see agx_sww_frame): node means of the vertex
+// slots, the storable-height mask at the nodes, centroid values as stored.
+__global__ void k_pool_sww_nodes(PoolDev d, int sid, int P, const int* off, const int* slot, const int* inv,
+                                 double msh, float* out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const PoolScn* S = d.scn + sid;
+  double aw = 0.0, az = 0.0, au = 0.0, av = 0.0;
+  const int a = off[p], b = off[p + 1];
+  for (int q = a; q < b; q++) {
+    const int s = slot[q];
+    const int ko = s / 3;
+    double w, z, uh, vh;
+    pool_vertex(d, S->P, S->cell0 + inv[ko], s - 3 * ko, w, z, uh, vh);
+    aw += w;
+    az += z;
+    au += uh;
+    av += vh;
+  }
+  if (b > a) {
+    const double k = (double)(b - a);
+    aw = aw / k;
+    az = az / k;
+    au = au / k;
+    av = av / k;
+  }
+  const bool storable = aw - az >= msh;
+  out[p] = (float)(storable ? aw : az);
+  out[P + p] = storable ? (float)au : 0.0f;
+  out[2 * P + p] = storable ? (float)av : 0.0f;
+}
+
+__global__ void k_pool_sww_cells(PoolDev d, int sid, const int* order, float* out) {
+  const PoolScn* S = d.scn + sid;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = S->ncell;
+  if (j >= n) return;
+  const int k = S->cell0 + j, o = order[j];
+  out[o] = (float)(d.wA[k] + d.z[k]);
+  out[n + o] = (float)d.uhA[k];
+  out[2 * n + o] = (float)d.vhA[k];
+}
+
 // update_timestep per scenario (one thread each).
 __global__ void k_pool_timestep(PoolDev d, int nscn) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nscn) return;
   PoolScn* S = d.scn + s;
   if (!S->alive || !S->active) return;
+  const unsigned long long key = S->clock.dt_key;
+  if (key) {                 // radius / speed of the selected cell in FP64
+    const int c = (int)(key & 0xffffffffull);
+    const double dt = d.radius[c] / (double)d.maxs[c];
+    S->clock.dt_key = ~(unsigned long long)__double_as_longlong(dt);
+  }
   S->clock.bfs[0] = S->clock.bfs_acc;
   timestep_logic(&S->clock);
 }
@@ -984,6 +1084,13 @@ __global__ void k_scatter_E(double* dst, const float4* E, int comp, const int* o
 // host side
 struct ScnHost {
   int alive = 0;
+  // sww output: node -> vertex-slot map (original order), device frame and its page-locked copy
+  int sww_P = 0;
+  int* sww_off = nullptr;
+  int* sww_slot = nullptr;
+  float* frame = nullptr;
+  float* frame_host = nullptr;
+  cudaEvent_t frame_done = nullptr;
   int N = 0, B = 0, tile0 = 0, ntile = 0, bnd0 = 0, halo0 = 0, nhalo = 0;
   agx_params prm{};
   int* order = nullptr;          // device [N]: original index of each stored cell
@@ -1068,6 +1175,7 @@ static size_t pool_layout(Pool* p, char* base) {
   double** dd[] = {&d.wA, &d.uhA, &d.vhA, &d.wB, &d.uhB, &d.vhB, &d.z};
   for (auto q : dd) *q = (double*)take(C * 8);
   d.area = (const double*)take(C * 8);
+  d.radius = (const double*)take(C * 8);
   d.eta = (float*)take(C * 4);
   d.W0 = (float4*)take(C * 16);
   d.W1 = (float4*)take(C * 16);
@@ -1093,6 +1201,18 @@ static size_t pool_layout(Pool* p, char* base) {
 using namespace agx;
 
 struct agx_pool_s : public agx::Pool {};
+
+static void free_sww(ScnHost& s) {
+  if (s.sww_off) cudaFree(s.sww_off);
+  if (s.sww_slot) cudaFree(s.sww_slot);
+  if (s.frame) cudaFree(s.frame);
+  if (s.frame_host) cudaFreeHost(s.frame_host);
+  if (s.frame_done) cudaEventDestroy(s.frame_done);
+  s.sww_off = s.sww_slot = nullptr;
+  s.frame = s.frame_host = nullptr;
+  s.frame_done = nullptr;
+  s.sww_P = 0;
+}
 
 static agx_status psync(Pool* p) {
   PCK(cudaStreamSynchronize(p->stream));
@@ -1152,6 +1272,7 @@ static void init_clock_p(Clock* c, const agx_params& p) {
   c->order = 2;
   c->default_order = 2;
   c->flux_timestep = p.evolve_max_timestep;
+  c->fluxcalls = p.timestepping_method;
 }
 
 static int nblk1(int n) { return (n + 255) / 256; }
@@ -1330,7 +1451,7 @@ int64_t agx_pool_footprint(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
 
 int64_t agx_pool_bytes_per_cell(void) {
   // static tables + FP64 state (2 buffers) + work records + explicit update
-  return 16 * 6 + 8 * 8 + 4 + 16 * 3 + 4 + 8 * 5;
+  return 16 * 6 + 8 * 9 + 4 + 16 * 3 + 4 + 8 * 5;
 }
 
 agx_status agx_pool_destroy(agx_pool p) {
@@ -1342,6 +1463,7 @@ agx_status agx_pool_destroy(agx_pool p) {
     if (s.order) cudaFree(s.order);
     if (s.inv) cudaFree(s.inv);
     if (s.series) cudaFree(s.series);
+    free_sww(s);
     for (auto& op : s.ops) if (op.idx) cudaFree((void*)op.idx);
   }
   if (p->arena) cudaFree(p->arena);
@@ -1365,16 +1487,17 @@ agx_status agx_pool_set_stream(agx_pool p, void* stream) {
 
 // Add a scenario.  conn [N*4] (neighbours in the stored order, boundary
 // -(m+1), meta word), geo [N*16] floats (g0 g1 g2 g3 blocks: jump matrix,
-// edge vectors, radius; dz and inv_area are filled here), area [N],
+// edge vectors, radius; dz and inv_area are filled here), area [N], the
+// FP64 radius [N] (the timestep quotient of the cell the CFL minimum selects),
 // order [N], boundary_cell [B] (stored order), lnk [N] (staging index of
 // each slot's neighbour), per tile halo_off/halo_cnt [ceil(N/TILE)] into
 // halo_cells [n_halo] (stored cell indices).
 agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, const float* geo,
-                        const double* area, const int32_t* order, const int32_t* bcell, const int32_t* lnk,
+                        const double* area, const double* radius, const int32_t* order, const int32_t* bcell, const int32_t* lnk,
                         const int32_t* halo_off, const int32_t* halo_cnt, int64_t n_halo,
                         const int32_t* halo_cells, const agx_params* prm, int32_t* sid_out) {
   AGX_TRACE("agx_pool_add");
-  if (!p || !conn || !geo || !area || !order || !prm || !sid_out || !lnk || !halo_off || !halo_cnt || N <= 0 ||
+  if (!p || !conn || !geo || !area || !radius || !order || !prm || !sid_out || !lnk || !halo_off || !halo_cnt || N <= 0 ||
       B < 0 || n_halo < 0)
     return pfail(AGX_E_INVALID, "bad arguments");
   if (prm->timestepping_method < 1 || prm->timestepping_method > 3)
@@ -1454,6 +1577,7 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
   const float4* gd[5] = {p->d.g0, p->d.g1, p->d.g2, p->d.g3, p->d.g4};
   for (int g = 0; g < 5; g++) PCK(cudaMemcpyAsync((void*)(gd[g] + c0), G[g].data(), N * 16, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync((void*)(p->d.area + c0), area, N * 8, cudaMemcpyHostToDevice, st));
+  PCK(cudaMemcpyAsync((void*)(p->d.radius + c0), radius, N * 8, cudaMemcpyHostToDevice, st));
   PCK(cudaMemcpyAsync((void*)(p->d.lnk + c0), lnk, N * 4, cudaMemcpyHostToDevice, st));
   {
     std::vector<int2> th(nt);
@@ -1552,6 +1676,7 @@ agx_status agx_pool_remove(agx_pool p, int32_t sid) {
   if (sh.order) cudaFree(sh.order);
   if (sh.inv) cudaFree(sh.inv);
   if (sh.series) cudaFree(sh.series);
+  free_sww(sh);
   bool had_ops = !sh.ops.empty();
   for (auto& op : sh.ops) if (op.idx) cudaFree((void*)op.idx);
   sh = ScnHost();
@@ -2066,6 +2191,8 @@ static void fill_stats_p(const Clock* c, agx_step_stats* o) {
   o->negative_cells = c->negative_cells;
   o->reason = c->reason;
   o->order = c->order;
+  o->boundary_flux_integral = c->bf_integral;
+  o->nonfinite_cells = c->nonfinite_cells;
 }
 
 // Advance every active scenario until each reaches its yield time, final
@@ -2134,12 +2261,83 @@ agx_status agx_pool_step_end(agx_pool p, int32_t* n_done) {
   return AGX_OK;
 }
 
+agx_status agx_pool_sww_bind(agx_pool p, int32_t sid, int64_t P, const int32_t* node_offsets,
+                             const int32_t* node_slots) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  const int64_t S3 = 3 * (int64_t)sh.N;
+  if (P < 0 || (P > 0 && (!node_offsets || !node_slots))) return pfail(AGX_E_INVALID, "bad arguments");
+  if (node_offsets[0] != 0 || node_offsets[P] != S3) return pfail(AGX_E_INVALID, "node offsets must run from 0 to 3N");
+  for (int64_t q = 0; q < P; q++)
+    if (node_offsets[q + 1] < node_offsets[q]) return pfail(AGX_E_INVALID, "node offsets must not decrease");
+  for (int64_t q = 0; q < S3; q++)
+    if (node_slots[q] < 0 || node_slots[q] >= S3) return pfail(AGX_E_INVALID, "vertex slot out of range");
+  agx_status st = psync(p);
+  if (st) return st;
+  free_sww(sh);
+  const size_t fbytes = ((size_t)3 * P + (size_t)S3) * 4 + 4;
+  PCK(cudaMalloc(&sh.sww_off, (size_t)(P + 1) * 4));
+  PCK(cudaMalloc(&sh.sww_slot, (size_t)S3 * 4 + 4));
+  PCK(cudaMalloc(&sh.frame, fbytes));
+  PCK(cudaMallocHost(&sh.frame_host, fbytes));
+  PCK(cudaEventCreateWithFlags(&sh.frame_done, cudaEventDisableTiming));
+  sh.sww_P = (int)P;
+  PCK(cudaMemcpyAsync(sh.sww_off, node_offsets, (size_t)(P + 1) * 4, cudaMemcpyHostToDevice, p->stream));
+  PCK(cudaMemcpyAsync(sh.sww_slot, node_slots, (size_t)S3 * 4, cudaMemcpyHostToDevice, p->stream));
+  return psync(p);
+}
+
+agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height) {
+  AGX_TRACE("agx_pool_sww_frame_async");
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  ScnHost& sh = p->scn[sid];
+  if (!sh.frame) return pfail(AGX_E_STATE, "agx_pool_sww_bind first");
+  agx_status st = ensure_work(p, sid);
+  if (st) return st;
+  cudaStream_t s = p->stream;
+  if (sh.sww_P > 0) {
+    k_pool_sww_nodes<<<nblk1(sh.sww_P), 256, 0, s>>>(p->d, sid, sh.sww_P, sh.sww_off, sh.sww_slot, sh.inv,
+                                                    min_storable_height, sh.frame);
+    count_launch();
+  }
+  k_pool_sww_cells<<<nblk1(sh.N), 256, 0, s>>>(p->d, sid, sh.order, sh.frame + 3 * (size_t)sh.sww_P);
+  count_launch();
+  PCK(cudaGetLastError());
+  PCK(cudaMemcpyAsync(sh.frame_host, sh.frame, ((size_t)3 * sh.sww_P + 3 * (size_t)sh.N) * 4,
+                      cudaMemcpyDeviceToHost, s));
+  PCK(cudaEventRecord(sh.frame_done, s));
+  return AGX_OK;
+}
+
+agx_status agx_pool_sww_frame_wait(agx_pool p, int32_t sid, const float** vertex, const float** centroid) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !vertex || !centroid)
+    return pfail(AGX_E_INVALID, "bad arguments");
+  ScnHost& sh = p->scn[sid];
+  if (!sh.frame_host) return pfail(AGX_E_STATE, "agx_pool_sww_bind first");
+  PCK(cudaEventSynchronize(sh.frame_done));
+  *vertex = sh.frame_host;
+  *centroid = sh.frame_host + 3 * (size_t)sh.sww_P;
+  return AGX_OK;
+}
+
+agx_status agx_pool_set_fixed_flux_timestep(agx_pool p, int32_t sid, double flux_timestep) {
+  if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
+  if (!(flux_timestep >= 0.0)) return pfail(AGX_E_INVALID, "flux_timestep needs to be greater than 0.0");
+  agx_status st = pull_scn(p, true);
+  if (st) return st;
+  p->scn_host[sid].clock.fixed_flux_dt = flux_timestep;
+  return push_scn(p);
+}
+
 agx_status agx_pool_get_stats(agx_pool p, int32_t sid, agx_step_stats* out) {
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive || !out) return pfail(AGX_E_INVALID, "bad scenario");
   agx_status st = pull_scn(p, true);
   if (st) return st;
   fill_stats_p(&p->scn_host[sid].clock, out);
   const int e = p->scn_host[sid].clock.error;
+  if (e & ERR_NONFINITE)
+    return pfail(AGX_E_NUMERIC, "non-finite conserved quantity (NaN or Inf) in %lld cell updates of scenario %d; "
+                 "its step loop stopped", (long long)p->scn_host[sid].clock.nonfinite_cells, sid);
   if (e & ERR_NUMERIC) return pfail(AGX_E_NUMERIC, "non-positive semi-implicit denominator");
   if (e & ERR_TIMESTEP) return pfail(AGX_E_TIMESTEP, "too small timestep at first order");
   if (e & ERR_NAN) return pfail(AGX_E_NUMERIC, "non-finite or non-positive timestep (state diverged)");

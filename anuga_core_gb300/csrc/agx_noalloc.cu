@@ -32,21 +32,25 @@ using agx::Riverwall;
 
 constexpr int NA_TPB = 256;
 constexpr long long NA_SLOTS = 3LL * AGX_NOALLOC_MAX_CELLS;
-constexpr long long NA_TAIL = 6 * NA_SLOTS;
+constexpr long long NA_STAMP = 6 * NA_SLOTS;              // u32 stamps, NA_SLOTS / 2 doubles
+constexpr long long NA_TAIL = NA_STAMP + NA_SLOTS / 2;
 constexpr int NA_MAX_DEVICES = 64;
 
 // Scratch, one copy per device (a __device__ variable exists on every device
 // the module is loaded on).  Layout in doubles: six slot arrays of NA_SLOTS
 // values each (flux components of w, uh, vh; wave speed; pressure flux; left
-// depth), then a tail of 32: [0] the timestep reduction key (u64 bits),
-// [1] the boundary flux sum, [2] a u64 flag set when a table index is out of
-// range.  The tail must start at zero on every call (k_na_reset); every slot
-// value read by the accumulation is written by the flux kernel of the same
-// call, so the slot arrays need no clearing.
-static __device__ __align__(256) double g_na_scratch[6 * NA_SLOTS + 32];
+// depth), then one 32-bit stamp per slot (the number of the call that last
+// wrote the slot), then a tail of 32: [0] the timestep reduction key (u64
+// bits), [1] the boundary flux sum, [2] u64 flags (1: a table index out of
+// range, 2: a slot the edge list did not write in this call), [3] the count
+// of slots written.  The tail must start at zero on every call (k_na_reset).
+// The slot arrays and stamps keep the last call's contents: the stamps show
+// which slots this call wrote, so they need no clearing either.
+static __device__ __align__(256) double g_na_scratch[NA_TAIL + 32];
 
 std::mutex g_na_mu;
 double* g_na_ptr[NA_MAX_DEVICES] = {};
+unsigned g_na_call[NA_MAX_DEVICES] = {};     // call number per device (stamps), never 0
 
 agx_status na_fail(agx_status code, char* err, int32_t err_len, const char* fmt, ...) {
   if (err && err_len > 0) {
@@ -60,7 +64,7 @@ agx_status na_fail(agx_status code, char* err, int32_t err_len, const char* fmt,
 
 // Address of the current device's scratch.  Looked up once per device, with
 // that device current; later calls read the cached pointer.
-agx_status na_scratch(double** out, char* err, int32_t err_len) {
+agx_status na_scratch(double** out, unsigned* call, char* err, int32_t err_len) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return na_fail(AGX_E_CUDA, err, err_len, "cudaGetDevice failed: %s", cudaGetErrorString(e));
@@ -77,6 +81,8 @@ agx_status na_scratch(double** out, char* err, int32_t err_len) {
     g_na_ptr[dev] = static_cast<double*>(p);
   }
   *out = g_na_ptr[dev];
+  if (++g_na_call[dev] == 0) g_na_call[dev] = 1;     // after 2^32 calls a stale stamp could match again
+  *call = g_na_call[dev];
   return AGX_OK;
 }
 
@@ -84,6 +90,7 @@ struct NaArgs {
   Params P;
   agx_flux_buffers b;
   int N, B, E;
+  unsigned call;       // stamp of this call
 };
 
 // Neighbour indices of a cell inside the mesh or the boundary, and
@@ -108,8 +115,11 @@ __global__ void k_na_reset(double* scr) {
   unsigned long long* t = reinterpret_cast<unsigned long long*>(scr + NA_TAIL);
   t[0] = 0ull;   // key: no timestep yet
   t[1] = 0ull;   // boundary flux sum: +0.0
-  t[2] = 0ull;   // no bad index
+  t[2] = 0ull;   // no bad index, no slot missed
+  t[3] = 0ull;   // slots written
 }
+
+__device__ __forceinline__ unsigned* na_stamps(double* scr) { return reinterpret_cast<unsigned*>(scr + NA_STAMP); }
 
 // One thread per listed edge: the flux from the listed slot's side, and its
 // exact negation for the slot on the other side (agx_plain.cu k_flux).
@@ -139,6 +149,7 @@ __global__ void k_na_flux(NaArgs a, double* scr) {
   scr[3 * NA_SLOTS + s] = R.speed;
   scr[4 * NA_SLOTS + s] = R.pflux;
   scr[5 * NA_SLOTS + s] = R.hleft;
+  na_stamps(scr)[s] = a.call;
   if (o >= 0) {
     scr[0 * NA_SLOTS + o] = -R.f[0];
     scr[1 * NA_SLOTS + o] = -R.f[1];
@@ -146,7 +157,9 @@ __global__ void k_na_flux(NaArgs a, double* scr) {
     scr[3 * NA_SLOTS + o] = R.speed;
     scr[4 * NA_SLOTS + o] = R.pflux;
     scr[5 * NA_SLOTS + o] = hr;
+    na_stamps(scr)[o] = a.call;
   }
+  atomicAdd(reinterpret_cast<unsigned long long*>(scr + NA_TAIL) + 3, o >= 0 ? 2ull : 1ull);
 }
 
 __device__ __forceinline__ double na_warp_sum(double x) {
@@ -173,8 +186,11 @@ __global__ void __launch_bounds__(NA_TPB) k_na_accum(NaArgs a, double* scr, int 
   if (k < a.N) {
     const int4* conn = reinterpret_cast<const int4*>(a.b.conn);
     const int4 c = conn[k];
+    const unsigned* stamp = na_stamps(scr);
     if (!na_cell_ok(c, a.N, a.B)) {
       atomicOr(na_flag(scr), 1ull);
+    } else if (stamp[3LL * k] != a.call || stamp[3LL * k + 1] != a.call || stamp[3LL * k + 2] != a.call) {
+      atomicOr(na_flag(scr), 2ull);       // a slot of this cell holds an earlier call's value
     } else {
       SlotResult R[3];
       int fn[3];
@@ -256,7 +272,8 @@ extern "C" agx_status agx_compute_fluxes_noalloc(const agx_params* p, const agx_
     return na_fail(AGX_E_INVALID, err, err_len, "conn must be 16-byte aligned (read as int4 rows)");
 
   double* scr = nullptr;
-  agx_status st = na_scratch(&scr, err, err_len);
+  unsigned call = 0;
+  agx_status st = na_scratch(&scr, &call, err, err_len);
   if (st != AGX_OK) return st;
 
   NaArgs a;
@@ -264,6 +281,7 @@ extern "C" agx_status agx_compute_fluxes_noalloc(const agx_params* p, const agx_
   a.N = (int)b->N;
   a.B = (int)b->B;
   a.E = (int)b->E;
+  a.call = call;
   Params& P = a.P;
   P.g = p->g;
   P.epsilon = p->epsilon;
@@ -295,11 +313,15 @@ extern "C" agx_status agx_compute_fluxes_noalloc(const agx_params* p, const agx_
   }
   if (e != cudaSuccess) return na_fail(AGX_E_CUDA, err, err_len, "kernel launch failed: %s", cudaGetErrorString(e));
   agx::count_launch(3);
-  unsigned long long tail[3] = {0ull, 0ull, 0ull};
+  unsigned long long tail[4] = {0ull, 0ull, 0ull, 0ull};
   e = cudaMemcpyAsync(tail, scr + NA_TAIL, sizeof(tail), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return na_fail(AGX_E_CUDA, err, err_len, "flux kernels failed: %s", cudaGetErrorString(e));
-  if (tail[2]) return na_fail(AGX_E_INVALID, err, err_len, "an edge-list or neighbour index is out of range");
+  if (tail[2] & 1ull) return na_fail(AGX_E_INVALID, err, err_len, "an edge-list or neighbour index is out of range");
+  if ((tail[2] & 2ull) || tail[3] != 3ull * (unsigned long long)b->N)
+    return na_fail(AGX_E_INVALID, err, err_len,
+                   "the edge list writes %llu slot results, not one for each of the 3N = %lld slots",
+                   tail[3], 3LL * (long long)b->N);
   double dt = p->evolve_max_timestep;
   if (substep == 0) {
     dt = 1.0e100;

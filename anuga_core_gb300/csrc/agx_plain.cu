@@ -249,7 +249,7 @@ __global__ void k_timestep(Dev d, int substep_count) {
 // 0.25 Q + 0.75 Q0; 3 RK3 last stage (2 Q + Q0) / 3 (generic_domain.py:2126, 2160-2166).
 __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int saxpy) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  int bad = 0, neg = 0;
+  int bad = 0, neg = 0, nf = 0;
   if (k < d.N) {
     const double dt = use_clock_dt ? d.clock->timestep : dt_arg;
     double w = d.w[k], uh = d.uh[k], vh = d.vh[k];
@@ -289,12 +289,20 @@ __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int 
     d.sw[k] = sw;
     d.suh[k] = suh;
     d.svh[k] = svh;
+    // a NaN or an infinity in the conserved state stops the step loop (the
+    // CFL minimum would otherwise skip the cell and let it spread)
+    nf = nonfinite64(w) | nonfinite64(uh) | nonfinite64(vh);
   }
   const int anyneg = __syncthreads_count(neg);
   const int anybad = __syncthreads_or(bad);
+  const int nnf = __syncthreads_count(nf);
   if (threadIdx.x == 0) {
     if (anyneg) atomicAdd((unsigned long long*)&d.clock->negative_cells, (unsigned long long)anyneg);
     if (anybad) atomicOr(&d.clock->error, (int)ERR_NUMERIC);
+    if (nnf) {
+      atomicAdd((unsigned long long*)&d.clock->nonfinite_cells, (unsigned long long)nnf);
+      atomicOr(&d.clock->error, (int)ERR_NONFINITE);
+    }
   }
 }
 
@@ -400,33 +408,42 @@ __global__ void __launch_bounds__(INLET_TPB) k_inlet(Dev d, RateOp op, int slot,
   if (threadIdx.x == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
 }
 
-// One sww frame (file/sww.py:352-368 store_timestep with smoothed vertex
-// values): per node the mean of its vertex slots, summed in slot order (as
-// numpy.bincount does), stage masked to the bed where the depth is below
-// minimum_storable_height; centroid values masked the same way; all as float.
+// One sww frame (file/sww.py:352-410 store_timestep with smoothed vertex
+// values): per node the mean of its vertex slots in the order the caller
+// gives (the reference's vertex_value_indices, summed as
+// quantity.c:823-870 _average_vertex_values does, total / k); a node is
+// storable when its mean stage minus its mean bed is at least
+// minimum_storable_height: otherwise the stage stored is the bed and the
+// momenta are zero.  Centroid values are stored as they are.  All as float.
 __global__ void k_sww_nodes(Dev d, int P, const int* off, const int* slot, double msh, float* out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
-  double aw = 0.0, au = 0.0, av = 0.0;
+  double aw = 0.0, az = 0.0, au = 0.0, av = 0.0;
   const int a = off[p], b = off[p + 1];
   for (int q = a; q < b; q++) {
     const int s = slot[q];
-    const double w = d.wv[s], z = d.zv[s];
-    aw += (w - z < msh) ? z : w;
+    aw += d.wv[s];
+    az += d.zv[s];
     au += d.uhv[s];
     av += d.vhv[s];
   }
-  const double c = b > a ? (double)(b - a) : 1.0;
-  out[p] = (float)(aw / c);
-  out[P + p] = (float)(au / c);
-  out[2 * P + p] = (float)(av / c);
+  if (b > a) {
+    const double k = (double)(b - a);
+    aw = aw / k;
+    az = az / k;
+    au = au / k;
+    av = av / k;
+  }
+  const bool storable = aw - az >= msh;
+  out[p] = (float)(storable ? aw : az);
+  out[P + p] = storable ? (float)au : 0.0f;
+  out[2 * P + p] = storable ? (float)av : 0.0f;
 }
 
-__global__ void k_sww_cells(Dev d, double msh, float* out) {
+__global__ void k_sww_cells(Dev d, float* out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.N) return;
-  const double w = d.w[k], z = d.z[k];
-  out[k] = (float)((w - z < msh) ? z : w);
+  out[k] = (float)d.w[k];
   out[d.N + k] = (float)d.uh[k];
   out[2 * d.N + k] = (float)d.vh[k];
 }
@@ -604,7 +621,7 @@ cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int i, double rate, 
 cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double msh) {
   const Dev& d = s->d;
   if (s->P > 0) LAUNCH(k_sww_nodes<<<nblk(s->P), TPB, 0, st>>>(d, s->P, s->node_off, s->node_slot, msh, s->frame));
-  if (d.N > 0) LAUNCH(k_sww_cells<<<nblk(d.N), TPB, 0, st>>>(d, msh, s->frame + 3 * (size_t)s->P));
+  if (d.N > 0) LAUNCH(k_sww_cells<<<nblk(d.N), TPB, 0, st>>>(d, s->frame + 3 * (size_t)s->P));
   return cudaSuccess;
 }
 

@@ -27,6 +27,7 @@ import numpy as np
 from . import _lib
 from .mesh import Mesh, rectangular_cross
 from .quantity import Quantity, DEVICE_FIELDS
+from .operators import boundary_flux_integral_operator
 from .tables import pack_tables
 
 EPSILON = 1.0e-12        # anuga/config.py:12
@@ -134,6 +135,15 @@ class Domain:
         self.quantities["x"].set_values(self.mesh.vertex_coordinates[:, 0].reshape(-1, 3))
         self.quantities["y"].set_values(self.mesh.vertex_coordinates[:, 1].reshape(-1, 3))
         self._mass_added_seen = 0.0
+        # boundary fluxes of the last step's stages, and their time integral
+        # (shallow_water_domain.py:380-387: the operator comes first among
+        # the fractional steps)
+        self.boundary_flux_sum = np.zeros(3)
+        self.boundary_flux_integral = boundary_flux_integral_operator(self)
+        self.volume_history = []
+        self.fixed_flux_timestep = None
+        # anuga/config.py:151 (generic_domain.py:331-332)
+        self.protect_against_isolated_degenerate_timesteps = False
 
     # ------------------------------------------------------------------
     # mesh accessors
@@ -266,6 +276,15 @@ class Domain:
             self.precision = precision
             self._invalidate_device()
 
+    def set_fixed_flux_timestep(self, flux_timestep=None):
+        """Disable variable timestepping with a fixed flux timestep, or
+        re-enable it with None (generic_domain.py:2332-2346)."""
+        if flux_timestep is not None and not flux_timestep > 0.0:
+            raise Exception("flux_timestep needs to be greater than 0.0")
+        self.fixed_flux_timestep = None if flux_timestep is None else float(flux_timestep)
+        if self._scn is not None:
+            self._scn.set_fixed_flux_timestep(self.fixed_flux_timestep)
+
     def set_evolve_max_timestep(self, t):
         self.evolve_max_timestep = float(t)
         self._invalidate_device()
@@ -392,8 +411,10 @@ class Domain:
 
     def _invalidate_device(self):
         if self._scn is not None:
+            self.flush_sww()
             # keep the device state: pull everything the host may not have yet
             self._pull([f for f in self._fstate])
+            self.boundary_flux_integral.fold_device()
             self._scn.close()
             self._scn = None
             for f in self._fstate:
@@ -436,6 +457,8 @@ class Domain:
             self._fstate[f] = _SYNCED
         self._bind_boundaries()
         self._bind_operators()
+        if self.fixed_flux_timestep is not None:
+            self._scn.set_fixed_flux_timestep(self.fixed_flux_timestep)
         return self._scn
 
     def _upload_fields(self):
@@ -563,6 +586,8 @@ class Domain:
                 return False
         if any(f is not manning_friction_implicit for f in self.forcing_terms):
             return False
+        if self.protect_against_isolated_degenerate_timesteps:
+            return False          # evaluated by the host between the phases of each step
         return True
 
     # ------------------------------------------------------------------
@@ -605,8 +630,33 @@ class Domain:
             else:
                 f(self)
 
+    def apply_protection_against_isolated_degenerate_timesteps(self):
+        """generic_domain.py:2520-2560: when the speed histogram (10 bins from
+        the minimum to the maximum speed) has cells in its top bin and none in
+        bins 4-8, the momenta of the cells above the top bin's edge are set
+        to zero.  Evaluated on the host from the device's max speeds."""
+        if self.protect_against_isolated_degenerate_timesteps is False:
+            return
+        speed = self.max_speed
+        if np.max(speed) < 10.0:
+            return
+        mx, mn = max(speed), min(speed)
+        bins = np.array([mn]) if mx == mn else np.arange(mn, mx, (mx - mn) / 10)
+        n = np.concatenate([np.searchsorted(np.sort(speed), bins), [len(speed)]], axis=0)
+        hist = n[1:] - n[:-1]
+        if len(hist) > 1 and hist[-1] > 0 and hist[4] == hist[5] == hist[6] == hist[7] == hist[8] == 0:
+            idx = np.nonzero(speed > bins[-1])[0]
+            for q in ("xmomentum", "ymomentum"):
+                c = self.quantities[q].centroid_values
+                c[idx] = 0.0
+                self._host_modified(DEVICE_FIELDS[q][0])
+            speed[idx] = 0.0          # the host's view only: the next flux call recomputes them
+
     def update_timestep(self, yieldstep, finaltime):
         """generic_domain.py:2349-2415."""
+        self.apply_protection_against_isolated_degenerate_timesteps()
+        if self.fixed_flux_timestep is not None:
+            self.flux_timestep = self.fixed_flux_timestep
         timestep = min(self.CFL * self.flux_timestep, self.evolve_max_timestep)
         self.recorded_max_timestep = max(timestep, self.recorded_max_timestep)
         self.recorded_min_timestep = min(timestep, self.recorded_min_timestep)
@@ -769,7 +819,8 @@ class Domain:
         if self.timestepping_method == "euler":
             self.relative_time = t0
         for op in self.fractional_step_operators:
-            op()
+            if op is not self.boundary_flux_integral:     # integrated by the device clock
+                op()
         self.relative_time = t1
         return 0 if reason == _lib.STOP_MAXSTEPS else reason
 
@@ -820,13 +871,16 @@ class Domain:
         self.distribute_to_vertices_and_edges()
         if self.store and (self.relative_time == 0.0 or not self.evolved_called):
             self._initialise_storage()
-        for t in self._evolve_base(yieldstep, finaltime, duration, skip_initial_step):
-            if self.store and self.yieldstep_counter % self.output_frequency == 0:
-                self.store_timestep()
-            if getattr(self, "checkpoint", False):
-                self._maybe_checkpoint()
-            yield t
-            self.yieldstep_counter += 1
+        try:
+            for t in self._evolve_base(yieldstep, finaltime, duration, skip_initial_step):
+                if self.store and self.yieldstep_counter % self.output_frequency == 0:
+                    self.store_timestep()
+                if getattr(self, "checkpoint", False):
+                    self._maybe_checkpoint()
+                yield t
+                self.yieldstep_counter += 1
+        finally:
+            self.flush_sww()
 
     # ------------------------------------------------------------------
     # checkpoint / resume (shallow_water_domain.py:1123-1157, :2376-2397;
@@ -965,9 +1019,48 @@ class Domain:
         return self._farr["max_speed"]
 
     def get_water_volume(self):
+        """Volume of water, sum of area x depth over the cells (and
+        appended to volume_history, shallow_water_domain.py:1630-1675)."""
         Q = self.quantities
-        h = Q["stage"].centroid_values - Q["elevation"].centroid_values
-        return float(np.sum(self.mesh.areas * h))
+        h = np.maximum(Q["stage"].centroid_values - Q["elevation"].centroid_values, 0.0)
+        volume = float(np.sum(self.mesh.areas * h))
+        self.volume_history.append(volume)
+        return volume
+
+    def get_boundary_flux_integral(self):
+        """Time integral of the flux through the boundaries since the start
+        (shallow_water_domain.py:1677-1700): positive for water that entered."""
+        return self.boundary_flux_integral.get_integral()
+
+    def get_fractional_step_volume_integral(self):
+        """Volume the fractional-step operators (rates, inlets) have added
+        (shallow_water_domain.py:1715-1745)."""
+        total = 0.0
+        for op in self.fractional_step_operators:
+            if hasattr(op, "get_Q"):
+                total += op.get_Q()
+            elif hasattr(op, "get_total_applied_volume"):
+                total += op.get_total_applied_volume()
+        return total
+
+    def report_water_volume_statistics(self, verbose=True, returnStats=False):
+        """Volume, boundary flux integral, fractional-step volume and their
+        balance against the first recorded volume (shallow_water_domain.py:2749-2781)."""
+        if not self.volume_history:
+            raise RuntimeError("call get_water_volume() at the start of the run first: the balance is "
+                               "taken against the first recorded volume")
+        vol = self.get_water_volume()
+        flux = self.get_boundary_flux_integral()
+        frac = self.get_fractional_step_volume_integral()
+        if verbose:
+            print(" ")
+            print("    Volume V is:", vol)
+            print("    Boundary Flux integral BF: ", flux)
+            print("    (rate + inlet) Fractional Step volume integral FS: ", frac)
+            print("    V - BF - FS - InitialVolume :", vol - flux - frac - self.volume_history[0])
+            print(" ")
+        if returnStats:
+            return [vol, flux, frac]
 
     def timestepping_statistics(self):
         return ("Time = %.4f, delta t in [%.8f, %.8f], steps=%d"
@@ -985,6 +1078,12 @@ class Domain:
     def store_timestep(self):
         if self.writer is not None:
             self.writer.store_timestep()
+
+    def flush_sww(self):
+        """Wait until the sww frames started so far are in the file (the
+        frames are copied and written while the next yieldstep runs)."""
+        if self.writer is not None:
+            self.writer.flush()
 
 
 def rectangular_cross_domain(*args, **kwargs):

@@ -35,7 +35,7 @@ def lib():
             "agx_pool_set_stream": ([H, ctypes.c_void_p], ctypes.c_int32),
             "agx_pool_set_state": ([H, ctypes.c_int32, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
             "agx_pool_get_state": ([H, ctypes.c_int32, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
-            "agx_pool_add": ([H, ctypes.c_int64, ctypes.c_int64, _i32p, _f32p, _f64p, _i32p, _i32p, _i32p,
+            "agx_pool_add": ([H, ctypes.c_int64, ctypes.c_int64, _i32p, _f32p, _f64p, _f64p, _i32p, _i32p, _i32p,
                               _i32p, _i32p, ctypes.c_int64, _i32p, P(_lib.Params), P(ctypes.c_int32)],
                              ctypes.c_int32),
             "agx_pool_remove": ([H, ctypes.c_int32], ctypes.c_int32),
@@ -54,6 +54,11 @@ def lib():
                                          ctypes.c_int32, ctypes.c_int32, _f64p], ctypes.c_int32),
             "agx_pool_clear_operators": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_set_fixed_flux_timestep": ([H, ctypes.c_int32, ctypes.c_double], ctypes.c_int32),
+            "agx_pool_sww_bind": ([H, ctypes.c_int32, ctypes.c_int64, _i32p, _i32p], ctypes.c_int32),
+            "agx_pool_sww_frame_async": ([H, ctypes.c_int32, ctypes.c_double], ctypes.c_int32),
+            "agx_pool_sww_frame_wait": ([H, ctypes.c_int32, P(ctypes.POINTER(ctypes.c_float)),
+                                         P(ctypes.POINTER(ctypes.c_float))], ctypes.c_int32),
             "agx_pool_set_clock": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int64], ctypes.c_int32),
             "agx_pool_deactivate": ([H, ctypes.c_int32], ctypes.c_int32),
@@ -137,7 +142,8 @@ class Pool:
         sid = ctypes.c_int32()
         hc = T["halo_cells"] if T["halo_cells"].size else np.zeros(1, np.int32)
         check(self.L.agx_pool_add(self.h, N, B, T["conn"].ctypes.data_as(_i32p), T["geo"].ctypes.data_as(_f32p),
-                                  T["area"].ctypes.data_as(_f64p), T["order"].ctypes.data_as(_i32p),
+                                  T["area"].ctypes.data_as(_f64p), T["radius"].ctypes.data_as(_f64p),
+                                  T["order"].ctypes.data_as(_i32p),
                                   T["boundary_cell"].ctypes.data_as(_i32p), T["lnk"].ctypes.data_as(_i32p),
                                   T["halo_off"].ctypes.data_as(_i32p), T["halo_cnt"].ctypes.data_as(_i32p),
                                   T["halo_cells"].size, hc.ctypes.data_as(_i32p), ctypes.byref(params),
@@ -217,6 +223,22 @@ class Pool:
         v = ctypes.c_double()
         check(self.L.agx_pool_operator_influx(self.h, sid, op, ctypes.byref(v)))
         return v.value
+
+    def sww_bind(self, sid, node_offsets, node_slots):
+        off = np.ascontiguousarray(node_offsets, np.int32)
+        sl = np.ascontiguousarray(node_slots, np.int32)
+        check(self.L.agx_pool_sww_bind(self.h, int(sid), off.size - 1, off.ctypes.data_as(_i32p),
+                                       sl.ctypes.data_as(_i32p)))
+
+    def sww_frame_async(self, sid, min_storable_height):
+        check(self.L.agx_pool_sww_frame_async(self.h, int(sid), float(min_storable_height)))
+
+    def sww_frame_wait(self, sid, P):
+        N, _ = self._keep[sid]
+        return _lib._frame_arrays(self.L.agx_pool_sww_frame_wait, (self.h, int(sid)), P, N)
+
+    def set_fixed_flux_timestep(self, sid, flux_timestep):
+        check(self.L.agx_pool_set_fixed_flux_timestep(self.h, int(sid), float(flux_timestep or 0.0)))
 
     def distribute(self, sid):
         check(self.L.agx_pool_distribute(self.h, sid))
@@ -415,6 +437,23 @@ class MixedScenario:
 
     def stats(self):
         return self.pool.stats(self.sid)
+
+    def set_fixed_flux_timestep(self, flux_timestep):
+        self.pool.set_fixed_flux_timestep(self.sid, flux_timestep)
+
+    def sww_bind(self, node_offsets, node_slots):
+        self.pool.sww_bind(self.sid, node_offsets, node_slots)
+        self._sww_P = len(node_offsets) - 1
+
+    def sww_frame_async(self, min_storable_height):
+        self.pool.sww_frame_async(self.sid, min_storable_height)
+
+    def sww_frame_wait(self):
+        return self.pool.sww_frame_wait(self.sid, self._sww_P)
+
+    def sww_frame(self, min_storable_height):
+        self.sww_frame_async(min_storable_height)
+        return self.sww_frame_wait()
 
     def set_stream(self, ptr):
         self.pool.set_stream(ptr)

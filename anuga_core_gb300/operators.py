@@ -2,7 +2,9 @@
 
 ``Rate_operator`` follows operators/rate_operators.py:149-258: after every
 full timestep, ``stage_c[idx] += factor * dt * rate`` (with the momentum
-scaling branch for negative rates).  ``Inlet_operator`` follows
+scaling branch for negative rates).  ``boundary_flux_integral_operator``
+follows operators/boundary_flux_integral_operator.py:20-62: the time
+integral of the boundary flux sums, which the Domain creates first.  ``Inlet_operator`` follows
 structures/inlet_operator.py:17-165: a discharge Q into an inlet region,
 filling its lowest cells to a level surface.  Both run on the device: with
 constant values inside the device step loop; given as functions of time, the
@@ -42,6 +44,74 @@ class Operator:
 
     def log_timestepping_statistics(self):
         pass
+
+
+class boundary_flux_integral_operator(Operator):
+    """Integral over time of the flux through the domain's boundaries
+    (operators/boundary_flux_integral_operator.py:20-62; created by the
+    Domain's constructor as shallow_water_domain.py:386-387 does).
+
+    After every step the integral grows by the step's boundary flux sums
+    weighted by its stages: dt b0 (euler), dt (b0 + b1) / 2 (rk2),
+    dt (b0 + b1 + 4 b2) / 6 (rk3).  Steps whose clock runs on the device
+    (the device step loop; every step of the mixed form) are integrated there;
+    steps the host drives phase by phase are integrated here, as the
+    reference does."""
+
+    device_loop = True
+
+    def __init__(self, domain, description=None, label=None, logging=False, verbose=False):
+        super().__init__(domain)
+        self.label = label or "boundary_flux_integral"
+        self._host = 0.0            # steps integrated on the host, and device totals folded in
+
+    def _device_part(self):
+        scn = self.domain._scn
+        if scn is None:
+            return 0.0
+        return float(scn.stats().boundary_flux_integral)
+
+    def fold_device(self):
+        """Move the device total into the host part (before the device
+        scenario is destroyed)."""
+        self._host += self._device_part()
+
+    def get_integral(self):
+        return self._host + self._device_part()
+
+    @property
+    def boundary_flux_integral(self):
+        return np.array([self.get_integral()])
+
+    def __call__(self):
+        """A step driven by the host, phase by phase (plain form)."""
+        d = self.domain
+        dt = d.timestep
+        b = np.array(d._scn.stats().boundary_flux_sum[:]) if d._scn is not None else d.boundary_flux_sum
+        m = d.timestepping_method
+        if m == "euler":
+            self._host = self._host + dt * b[0]
+        elif m == "rk2":
+            self._host = self._host + 0.5 * dt * (b[0] + b[1])
+        elif m == "rk3":
+            self._host = self._host + 1.0 / 6.0 * dt * (b[0] + b[1] + 4.0 * b[2])
+        else:
+            raise Exception("Cannot compute boundary flux integral with this timestepping method")
+        d.boundary_flux_sum = np.zeros(3)
+
+    def __getstate__(self):
+        state = self.__dict__.copy()
+        state["_host"] = self.get_integral()     # the restored domain's device clock starts at zero
+        return state
+
+    def parallel_safe(self):
+        return True
+
+    def statistics(self):
+        return self.label + ": Boundary_flux_integral operator"
+
+    def timestepping_statistics(self):
+        return "    " + self.label + ": Integrating the boundary flux"
 
 
 class Rate_operator(Operator):

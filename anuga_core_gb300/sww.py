@@ -1,23 +1,28 @@
 """SWW (NetCDF) output of a Domain at yieldsteps.
 
-Follows the layout written by the reference's ``file/sww.py`` (SWW_file,
-Write_sww: dimensions number_of_volumes / number_of_vertices /
-number_of_points / number_of_timesteps; variables x, y, volumes, time,
-elevation, friction, stage, xmomentum, ymomentum in single precision, the
-``*_c`` centroid variables when centroids are stored, and the
-``minimum_storable_height`` mask on stage, file/sww.py:352-368).  Vertex
-values are stored smoothed (averaged per node), the reference's default
-(``set_store_vertices_uniquely(False)``).
+Follows what the reference's ``file/sww.py`` writes (SWW_file, Write_sww:
+dimensions number_of_volumes / number_of_vertices / number_of_points /
+number_of_timesteps; variables x, y, volumes, time, elevation, friction,
+stage, xmomentum, ymomentum in single precision, their ``*_range`` and the
+``*_c`` centroid variables).  A frame is formed as SWW_file.store_timestep
+does (file/sww.py:352-410): per node the mean of its vertex values, summed in
+the order of the mesh's vertex_value_indices (general_mesh.py:830, the
+default numpy argsort of the triangles; quantity.c:823-870 divides the sum by
+the count); where the mean stage minus the mean bed is below
+minimum_storable_height the node's stage is its bed and its momenta are zero;
+centroid values are stored as they are.
 
-On the plain FP64 form the frame is formed on the device (agx_sww_frame:
-storable-height mask, node means summed in the same order as numpy's
-bincount, single precision) and read back with one copy of 3 floats per node
-and 3 per cell; the mixed form builds it on the host from the quantities'
-vertex values.  NetCDF classic format is written with scipy.io.netcdf_file
-(the netCDF4 package is not required).
+Both forms build the frame on the device (agx_sww_frame_async: node means,
+mask and conversion to single precision in one kernel pair) and copy it into
+page-locked memory without blocking the host.  The netCDF append then runs
+on a writer thread while the host issues the next yieldstep; the file is
+complete once the next frame starts, when evolve returns, or after
+``flush()``.  NetCDF classic format is written with scipy.io.netcdf_file (the
+netCDF4 package is not required).
 """
 from __future__ import annotations
 
+import concurrent.futures
 import os
 
 import numpy as np
@@ -27,45 +32,87 @@ DYNAMIC = ("stage", "xmomentum", "ymomentum")
 
 
 class SWW_file:
-    def __init__(self, domain, store_centroids=True):
+    def __init__(self, domain, store_centroids=True, asynchronous=True):
         from scipy.io import netcdf_file
         self.domain = domain
         self.filename = os.path.join(domain.datadir, domain.get_name() + ".sww")
         self.store_centroids = store_centroids
+        self.asynchronous = asynchronous
         self._netcdf_file = netcdf_file
         mesh = domain.mesh
-        tri = mesh.triangles
+        tri = np.asarray(mesh.triangles, np.int64)
         self.N = len(tri)
         self.P = mesh.number_of_nodes
         self._tri = tri
-        self._count = np.bincount(tri.ravel(), minlength=self.P).astype(float)
-        self._count[self._count == 0] = 1.0
+        flat = tri.ravel()
+        self._counts = np.bincount(flat, minlength=self.P)
+        # vertex slots grouped by node, in the order of the reference's
+        # vertex_value_indices
+        self._vvi = np.argsort(flat).astype(np.int64)
+        self._off = np.zeros(self.P + 1, np.int64)
+        self._off[1:] = np.cumsum(self._counts)
+        self._exec = None
+        self._pending = None
 
     def __getstate__(self):
+        self.flush()
         state = self.__dict__.copy()
         state.pop("_bound_to", None)
+        state["_exec"] = None
+        state["_pending"] = None
         return state
 
-    def _device_frame(self):
-        """(vertex [3, P], centroid [3, N]) float32 from the device, or None."""
+    # ------------------------------------------------------------------
+    def _device_scn(self):
+        """The domain's device scenario, bound to this file's node map."""
         d = self.domain
         scn = d._scn
-        if scn is None or not hasattr(scn, "sww_frame"):
+        if scn is None or not hasattr(scn, "sww_frame_async"):
             return None
         if getattr(self, "_bound_to", None) is not scn:      # a new device scenario needs the node map
-            slots = np.argsort(self._tri.ravel(), kind="stable")
-            counts = np.bincount(self._tri.ravel(), minlength=self.P)
-            off = np.zeros(self.P + 1, np.int64)
-            off[1:] = np.cumsum(counts)
-            scn.sww_bind(off, slots)
+            scn.sww_bind(self._off, self._vvi)
             self._bound_to = scn
         d._push_dirty()
-        return scn.sww_frame(d.minimum_storable_height)
+        return scn
+
+    def _device_frame(self):
+        """(vertex [3, P], centroid [3, N]) float32 formed on the device, or None."""
+        scn = self._device_scn()
+        if scn is None:
+            return None
+        self.flush()
+        scn.sww_frame_async(self.domain.minimum_storable_height)
+        return scn.sww_frame_wait()
 
     def _smooth(self, vertex_values):
-        acc = np.bincount(self._tri.ravel(), weights=vertex_values.ravel(), minlength=self.P)
-        return acc / self._count
+        """Node means of vertex values as quantity.c:823-870 forms them: the
+        node's vertex values added one at a time in vertex_value_indices
+        order, the total divided by their count."""
+        v = np.asarray(vertex_values, float).ravel()[self._vvi]
+        acc = np.zeros(self.P)
+        start = self._off[:-1]
+        for j in range(int(self._counts.max()) if self.P else 0):
+            sel = self._counts > j
+            acc[sel] = acc[sel] + v[start[sel] + j]
+        nz = self._counts > 0
+        acc[nz] = acc[nz] / self._counts[nz]
+        return acc
 
+    def host_frame(self):
+        """The same frame formed on the host from the quantities."""
+        d = self.domain
+        Q = d.quantities
+        wn = self._smooth(Q["stage"].vertex_values)
+        zn = self._smooth(Q["elevation"].vertex_values)
+        storable = wn - zn >= d.minimum_storable_height
+        V = [np.where(storable, wn.astype(np.float32), zn.astype(np.float32)).astype(np.float32)]
+        for q in ("xmomentum", "ymomentum"):
+            A = self._smooth(Q[q].vertex_values).astype(np.float32)
+            V.append(np.where(storable, A, np.float32(0.0)).astype(np.float32))
+        C = [Q[q].centroid_values.astype(np.float32) for q in DYNAMIC]
+        return np.array(V), np.array(C)
+
+    # ------------------------------------------------------------------
     def store_connectivity(self):
         d = self.domain
         f = self._netcdf_file(self.filename, "w", version=2)
@@ -86,70 +133,64 @@ class SWW_file:
         f.createVariable("time", "d", ("number_of_timesteps",))
         for q in STATIC:
             v = f.createVariable(q, "f", ("number_of_points",))
-            v[:] = self._smooth(d.quantities[q].vertex_values).astype(np.float32)
+            A = self._smooth(d.quantities[q].vertex_values).astype(np.float32)
+            v[:] = A
             r = f.createVariable(q + "_range", "f", ("numbers_in_range",))
-            vals = d.quantities[q].centroid_values
-            r[:] = np.array([vals.min(), vals.max()], np.float32) if vals.size else np.zeros(2, np.float32)
+            r[:] = np.array([A.min(), A.max()], np.float32) if A.size else np.zeros(2, np.float32)
             if self.store_centroids:
                 c = f.createVariable(q + "_c", "f", ("number_of_volumes",))
-                c[:] = vals.astype(np.float32)
+                c[:] = d.quantities[q].centroid_values.astype(np.float32)
+        big = np.finfo(np.float32).max
         for q in DYNAMIC:
             f.createVariable(q, "f", ("number_of_timesteps", "number_of_points"))
             r = f.createVariable(q + "_range", "f", ("numbers_in_range",))
-            r[:] = np.array([np.inf, -np.inf], np.float32)
+            r[:] = np.array([big, -big], np.float32)
             if self.store_centroids:
                 f.createVariable(q + "_c", "f", ("number_of_timesteps", "number_of_volumes"))
         f.close()
 
-    def store_timestep(self):
-        d = self.domain
+    def _append(self, t, V, C):
         f = self._netcdf_file(self.filename, "a", version=2)
-        t = f.variables["time"]
-        i = t.shape[0]
-        t[i] = d.get_time() - d.starttime
-        frame = self._device_frame()
-        Q = d.quantities
-        zv = Q["elevation"].vertex_values if frame is None else None
+        tv = f.variables["time"]
+        i = tv.shape[0]
+        tv[i] = t
         for j, q in enumerate(DYNAMIC):
-            if frame is not None:
-                A = frame[0][j]
-            else:
-                vv = Q[q].vertex_values
-                if q == "stage":
-                    # minimum_storable_height mask (file/sww.py:352-368)
-                    vv = np.where(vv - zv < d.minimum_storable_height, zv, vv)
-                A = self._smooth(vv).astype(np.float32)
+            A = V[j]
             f.variables[q][i, :] = A
             r = f.variables[q + "_range"]
-            r[0] = min(float(r[0]), float(A.min()) if A.size else np.inf)
-            r[1] = max(float(r[1]), float(A.max()) if A.size else -np.inf)
+            if A.size:
+                r[0] = min(float(r[0]), float(A.min()))
+                r[1] = max(float(r[1]), float(A.max()))
             if self.store_centroids:
-                if frame is not None:
-                    c = frame[1][j]
-                else:
-                    c = Q[q].centroid_values
-                    if q == "stage":
-                        zc = Q["elevation"].centroid_values
-                        c = np.where(c - zc < d.minimum_storable_height, zc, c)
-                f.variables[q + "_c"][i, :] = np.asarray(c, np.float32)
+                f.variables[q + "_c"][i, :] = C[j]
         f.close()
 
-    def host_frame(self):
-        """The same frame formed on the host from the quantities (reference)."""
+    def _write_device_frame(self, t, scn):
+        V, C = scn.sww_frame_wait()
+        self._append(t, V, C)
+
+    def store_timestep(self):
         d = self.domain
-        Q = d.quantities
-        zv = Q["elevation"].vertex_values
-        zc = Q["elevation"].centroid_values
-        V, C = [], []
-        for q in DYNAMIC:
-            vv = Q[q].vertex_values
-            c = Q[q].centroid_values
-            if q == "stage":
-                vv = np.where(vv - zv < d.minimum_storable_height, zv, vv)
-                c = np.where(c - zc < d.minimum_storable_height, zc, c)
-            V.append(self._smooth(vv).astype(np.float32))
-            C.append(c.astype(np.float32))
-        return np.array(V), np.array(C)
+        t = d.get_time() - d.starttime
+        self.flush()
+        scn = self._device_scn()
+        if scn is None:
+            V, C = self.host_frame()
+            self._append(t, V, C)
+            return
+        scn.sww_frame_async(d.minimum_storable_height)
+        if self.asynchronous:
+            if self._exec is None:
+                self._exec = concurrent.futures.ThreadPoolExecutor(max_workers=1)
+            self._pending = self._exec.submit(self._write_device_frame, t, scn)
+        else:
+            self._write_device_frame(t, scn)
+
+    def flush(self):
+        """Wait until the last frame is in the file (raises its error, if any)."""
+        if self._pending is not None:
+            fut, self._pending = self._pending, None
+            fut.result()
 
 
 def read_sww(filename):

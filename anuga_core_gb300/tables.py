@@ -162,8 +162,8 @@ def pack_mixed_numpy(mesh, order=None):
     Returns conn int32 [N,4] (neighbours in the stored order, boundary edges as
     -(m+1) with the mesh's boundary index m, meta word), geo float32 [N,16]
     (jump matrix M row-major in g0.xyzw g1.xyzw g2.x, edge vectors in
-    g2.yzw g3.xyz, radius in g3.w), area [N], order [N] (original index of each
-    stored cell) and boundary_cell [B] (stored index).
+    g2.yzw g3.xyz, radius in g3.w), area [N], radius [N] (FP64), order [N]
+    (original index of each stored cell) and boundary_cell [B] (stored index).
 
     The jump matrix maps the differences to the three surrogate neighbours,
     Dq_j = q_{s_j} - q_k, to the provisional edge jumps; it is the linear
@@ -242,6 +242,7 @@ def pack_mixed_numpy(mesh, order=None):
     return dict(conn=conn_s, lnk=lnk, halo_off=hoff, halo_cnt=hcnt, halo_cells=hcells,
                 geo=np.ascontiguousarray(geo[order]),
                 area=np.ascontiguousarray(np.asarray(mesh.areas, np.float64)[order]),
+                radius=np.ascontiguousarray(np.asarray(mesh.radii, np.float64)[order]),
                 order=np.ascontiguousarray(order.astype(np.int32)),
                 boundary_cell=np.ascontiguousarray(bcell.astype(np.int32)))
 
@@ -448,4 +449,5 @@ def pack_mixed(mesh, order=None):
     bcell = inv[np.asarray(mesh.boundary_cells, np.int64)]
     lnk, hoff, hcnt, hcells = tile_halos(conn_s)
     return dict(conn=conn_s, lnk=lnk, halo_off=hoff, halo_cnt=hcnt, halo_cells=hcells, geo=geo, area=area_s,
+                radius=np.ascontiguousarray(np.asarray(mesh.radii, np.float64)[order]),
                 order=order_s, boundary_cell=np.ascontiguousarray(bcell.astype(np.int32)))

@@ -12,7 +12,13 @@ the 129 MB L2, so no explicit flush is needed between steps.
 By default the plain FP64 path and then the mixed-precision path run on the
 same workload; the line's value, roofline and e2e are the mixed path's, and
 `plain_fp64` holds the plain path's figures (`mixed_over_plain` = ratio).
-`--workload batch` and `--workload serve` run the batched and serving forms.
+`accuracy` holds the mixed path's error against the plain FP64 path after
+2000 mixed steps of the same workload, at the same simulated time (max depth
+and velocity error, relative volume difference); `batched` the batched form
+(256 scenarios, ~20M triangles, one pool, 500 timed steps) with its error on
+a sample of scenarios; `serving` the serving form (256 requests of a Poisson
+stream, p50/p99 latency).  `--workload batch` and `--workload serve` run the
+batched and serving forms alone.
 
 `--impl reference` times the CPU oracle (the restated reference algorithm,
 OpenMP over all host cores) on a bounded sample of the same workload.
@@ -136,7 +142,7 @@ def _oracle_domain(m, threads, workload="inflow_bumps", cells=1.2e6):
     if workload == "rain_polygon":
         d = workloads.rain_polygon(target_cells=cells, precision="fp64")
         kinds = {"inflow": ("dirichlet", (3.0, 0.0, 0.0)), "wall": ("reflective", None)}
-        rates = [(op.indices, op.rate) for op in d.fractional_step_operators]
+        rates = [(op.indices, op.rate) for op in d.fractional_step_operators if hasattr(op, "rate")]
     else:
         d = workloads.inflow_bumps(m=m)
         kinds = {"left": ("dirichlet", (2.0, 0.0, 0.0)), "right": ("transmissive", None),
@@ -213,7 +219,13 @@ def main():
                     help="both: plain FP64 then mixed on the same workload; the line's value is mixed")
     ap.add_argument("--cpu-steps", type=int, default=60, dest="cpu_steps")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--requests", type=int, default=64, help="serve workload: number of requests")
+    ap.add_argument("--requests", type=int, default=256, help="serve workload: number of requests")
+    ap.add_argument("--err-steps", type=int, default=2000, dest="err_steps",
+                    help="mixed steps of the accuracy check against plain FP64 (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=500, dest="batch_steps",
+                    help="timed steps of the batched form in the default line")
+    ap.add_argument("--no-batch", action="store_true", help="leave the batched form out of the default line")
+    ap.add_argument("--no-serve", action="store_true", help="leave the serving form out of the default line")
     ap.add_argument("--cells", type=float, default=1.2e6, help="rain_polygon workload: target triangles")
     ap.add_argument("--workload", default="inflow_bumps", choices=["inflow_bumps", "rain_polygon", "batch", "serve"],
                     help="inflow_bumps: one 4M-triangle mesh; batch: 256 scenarios (~20M triangles) in one pool")
@@ -260,6 +272,15 @@ def main():
     for prec in precisions:
         res[prec] = measure_single(args, prec, torch, world, barrier, dist, builder)
     clocks = sampler.stop()
+    both = args.precision == "both"
+    accuracy = measure_accuracy(args, builder) if both and args.err_steps > 0 else None
+    batched = serving = None
+    if both and args.workload == "inflow_bumps":
+        if not args.no_batch:
+            batched = measure_batch(args, torch, world, dist, args.batch_steps, err_sample=args.batch_count)
+            batched["over_plain_fp64"] = batched["value"] / res["fp64"]["value"]
+        if not args.no_serve and world == 1:
+            serving = measure_serve(args, torch)
     if rank == 0:
         head = res[precisions[-1]]
         N = head["cells"]
@@ -285,6 +306,15 @@ def main():
             pf = res["fp64"]
             line["plain_fp64"] = {k: pf[k] for k in ("value", "ms_per_step", "roofline", "step_roofline", "e2e")}
             line["mixed_over_plain"] = head["value"] / pf["value"]
+        if accuracy is not None:
+            line["accuracy"] = accuracy
+            for k in ("max_depth_err_m", "max_velocity_err_ms", "rel_volume_err"):
+                line[k] = accuracy[k]
+        if batched is not None:
+            line["batched"] = batched
+            line["gpu_launches"] += int(batched.get("gpu_launches", 0))
+        if serving is not None:
+            line["serving"] = serving
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -362,8 +392,7 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
         fp = _lib.fp64_throughput()
         roof["fp64_measured"] = fp
         roof["note"] = ("FP64-pipe bound: the measured FP64 rates (fp64_measured, G ops/s) are 1/54 of the FP32 "
-                        "rate; ncu shows the extrapolation kernel's FP64 pipe 84% busy at 6% of HBM bandwidth "
-                        "(profiles/k_extrap_inflow_bumps_1M_fp64.md)")
+                        "rate; ncu shows the extrapolation kernel's FP64 pipe 84% busy at 6% of HBM bandwidth")
     alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
     ach_s = alg_step / (ms_per_step / 1e3) / 1e9
     step_roof = {"achieved": ach_s, "peak": hbm, "unit": "GB/s", "frac": ach_s / hbm,
@@ -408,19 +437,59 @@ TRAFFIC_PER_STEP = {
         "bytes_per_cell": (117.617408e6 + 10.710272e6 + 169.683968e6 + 23.024640e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
                 "(m=500, MINB=8 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
-                "scaled by cells; profiles/k_pool_flux_inflow_bumps_1M_mixed.md"},
+                "scaled by cells"},
     ("fp64", "extrap"): {
         "bytes_per_cell": 2 * (125.701632e6 + 78.489088e6) / 1.0e6,
         "note": "ncu --set full of k_extrap<0> (edges only, flowing state) on the 1.0M-triangle inflow_bumps "
                 "case (m=500), dram__bytes_read.sum + dram__bytes_write.sum per launch x 2 launches per "
-                "DE1 step, scaled by cells; profiles/k_extrap_inflow_bumps_1M_fp64.md"},
+                "DE1 step, scaled by cells"},
 }
 
 
-def run_batch(args, torch, rank, world, local, dist):
+def measure_accuracy(args, builder):
+    """Error of the mixed form against the plain FP64 form on the same
+    workload: the mixed form takes `err_steps` steps from the protected
+    initial state; the plain form evolves to the same simulated time.
+    Max depth error, max velocity error over cells wetter than 1 cm in both,
+    and the relative difference of the water volumes."""
+    t0 = time.time()
+    dm = builder("mixed")
+    dm.distribute_to_vertices_and_edges()
+    st = dm.advance_steps(args.err_steps)
+    T = st.time
+    Qm = dm.quantities
+    wm, um, vm = (Qm[q].centroid_values.copy() for q in ("stage", "xmomentum", "ymomentum"))
+    dm._scn.close()
+    dm._scn = None
+    dp = builder("fp64")
+    for _ in dp.evolve(yieldstep=T, finaltime=T):
+        pass
+    Qp = dp.quantities
+    z = Qp["elevation"].centroid_values
+    wp, up, vp = (Qp[q].centroid_values for q in ("stage", "xmomentum", "ymomentum"))
+    hm, hp = np.maximum(wm - z, 0.0), np.maximum(wp - z, 0.0)
+    wet = (hm > 0.01) & (hp > 0.01)
+    dvel = max(float(np.abs(um[wet] / hm[wet] - up[wet] / hp[wet]).max()),
+               float(np.abs(vm[wet] / hm[wet] - vp[wet] / hp[wet]).max())) if wet.any() else 0.0
+    A = dp.mesh.areas
+    vol_m, vol_p = float(np.sum(A * hm)), float(np.sum(A * hp))
+    out = {"max_depth_err_m": float(np.abs(hm - hp).max()), "max_velocity_err_ms": dvel,
+           "rel_volume_err": abs(vol_m - vol_p) / max(vol_p, 1e-300),
+           "mixed_steps": int(args.err_steps), "plain_steps": int(dp.total_steps), "simulated_s": T,
+           "wet_cells_compared": int(wet.sum()), "bound_m": 1.0e-3,
+           "against": "plain FP64 path (bit-exact with the reference's FP64 DE1 step) at the same simulated time",
+           "wall_s": time.time() - t0}
+    dp._scn.close()
+    dp._scn = None
+    return out
+
+
+def measure_batch(args, torch, world, dist, steps, err_sample=0):
     """256 independent scenarios (mesh sides log-uniform in [20, 400], ~20M
     triangles) in one device pool, mixed precision, all advanced by the same
-    persistent kernels and one graph launch per call."""
+    persistent kernels and one graph launch per call.  With err_sample > 0,
+    that many scenarios (evenly spaced) are also run alone in plain FP64 to
+    the same simulated time and their max depth error is reported."""
     from anuga_core_gb300 import workloads, _lib
     from anuga_core_gb300.batch import Batch
     t0 = time.time()
@@ -435,49 +504,105 @@ def run_batch(args, torch, rank, world, local, dist):
     res, best = tune_pool(B.pool, steps=3, reps=2)
     B.advance_steps(args.warmup)
     launches0 = _lib.kernel_launches()
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    B.advance_steps(args.steps)
+    B.advance_steps(steps)
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
     ms = max_over_ranks(e0.elapsed_time(e1), dist)
     launches = _lib.kernel_launches() - launches0
     phases = B.pool.time_phases(reps=2)
-    value = replica_value(N, args.steps, ms, world)
+    value = replica_value(N, steps, ms, world)
     hbm, peak_kind = _peaks()
-    ach = ALG_BYTES_PER_CELL_STEP["mixed"] * N / (ms / args.steps / 1e3) / 1e9
+    ach = ALG_BYTES_PER_CELL_STEP["mixed"] * N / (ms / steps / 1e3) / 1e9
     dominant = max(phases, key=phases.get)
     kb = KERNEL_BYTES_PER_CELL["mixed"].get(dominant)
     ach_k = kb * N / (phases[dominant] / 1e3) / 1e9 if kb else None
     tr = TRAFFIC_PER_STEP.get(("mixed", dominant))
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
-            "config": {"workload": "batch of %d rectangular-cross scenarios, sides log-uniform [20,400], %d triangles, "
+    out = {"value": value, "unit": UNIT, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+           "workload": "batch of %d rectangular-cross scenarios, sides log-uniform [20,400], %d triangles, "
                        "DE1 mixed, one pool" % (len(doms), N), "cells": N, "scenarios": len(doms),
-                       "setup_s": setup_s, "draw": info["draw"], "l2": "inputs larger than L2",
-                       "autotune": {"chosen": best, "s_per_step": res}},
-            "roofline": {"bound": "hbm", "achieved": ach_k, "peak": hbm, "unit": "GB/s",
-                         "frac": ach_k / hbm if ach_k else None, "peak_kind": peak_kind,
-                         "traffic": tr["bytes_per_cell"] * N if tr else None,
-                         "traffic_note": tr["note"] if tr else None,
-                         "kernel": "%s (%.1f%% of step time)" % (dominant, 100.0 * phases[dominant] / max(sum(phases.values()), 1e-9)),
-                         "kernel_ms_per_step": phases[dominant], "alg_bytes_per_cell": kb, "phase_ms": phases},
-            "step_roofline": {"achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                              "note": "352 algorithmic B/cell-step of the ideal fused step x cells / step time"},
-            "gpu_launches": int(launches), "clocks": clocks}
+           "setup_s": setup_s, "draw": info["draw"], "autotune": {"chosen": best, "s_per_step": res},
+           "roofline": {"bound": "hbm", "achieved": ach_k, "peak": hbm, "unit": "GB/s",
+                        "frac": ach_k / hbm if ach_k else None, "peak_kind": peak_kind,
+                        "traffic": tr["bytes_per_cell"] * N if tr else None,
+                        "traffic_note": tr["note"] if tr else None,
+                        "kernel": "%s (%.1f%% of step time)" % (dominant, 100.0 * phases[dominant] / max(sum(phases.values()), 1e-9)),
+                        "kernel_ms_per_step": phases[dominant], "alg_bytes_per_cell": kb, "phase_ms": phases},
+           "step_roofline": {"achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "note": "352 algorithmic B/cell-step of the ideal fused step x cells / step time"},
+           "gpu_launches": int(launches), "clocks": clocks}
+    if err_sample > 0:
+        # each checked scenario alone in plain FP64 to the same time (no yields
+        # in either run); where the depth differs by more than 1 mm, the FP64
+        # run is repeated with ten yields to show how far the FP64 solution
+        # itself moves when only its timestep sequence changes
+        t1 = time.time()
+        pick = np.unique(np.linspace(0, len(doms) - 1, err_sample).round().astype(int))
+        worst = [0.0, 0.0]
+        over = []
+
+        def plain(i, T, yields):
+            dp = workloads.batch_scenario(info["sides"][i], 42 * 1000 + int(i), "dam" if i % 2 == 0 else "inflow",
+                                          precision="fp64")
+            for _ in dp.evolve(yieldstep=T / yields, finaltime=T):
+                pass
+            z = dp.quantities["elevation"].centroid_values
+            h = np.maximum(dp.quantities["stage"].centroid_values - z, 0.0)
+            A = dp.mesh.areas
+            dp._scn.close()
+            dp._scn = None
+            return h, z, A
+
+        for i in pick:
+            st = B.stats(int(i))
+            got = B.get_centroids(int(i))
+            hp, z, A = plain(int(i), st.time, 1)
+            hm = np.maximum(got["stage_c"] - z, 0.0)
+            e = float(np.abs(hm - hp).max())
+            vol = abs(float(np.sum(A * hm)) - float(np.sum(A * hp))) / max(float(np.sum(A * hp)), 1e-300)
+            worst[1] = max(worst[1], vol)
+            if e > 1.0e-3:
+                h10 = plain(int(i), st.time, 10)[0]
+                over.append({"scenario": int(i), "max_depth_err_m": e,
+                             "fp64_spread_m": float(np.abs(h10 - hp).max())})
+            else:
+                worst[0] = max(worst[0], e)
+        out["accuracy"] = {"max_depth_err_m": max([worst[0]] + [o["max_depth_err_m"] for o in over]),
+                           "max_depth_err_within_bound_m": worst[0], "rel_volume_err": worst[1],
+                           "scenarios_checked": int(len(pick)), "scenarios_over_1mm": over,
+                           "against": "each scenario alone in plain FP64 at the same simulated time, same "
+                                      "(yield-free) timestep sequence; fp64_spread_m = how far the FP64 "
+                                      "solution moves when run with ten yields instead",
+                           "wall_s": time.time() - t1}
+    B.close()
+    torch.cuda.set_stream(torch.cuda.default_stream())
+    return out
+
+
+def run_batch(args, torch, rank, world, local, dist):
+    """The batched form alone: 256 scenarios in one pool (see measure_batch)."""
+    b = measure_batch(args, torch, world, dist, args.steps, err_sample=0)
+    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
+            "config": {"workload": b["workload"], "cells": b["cells"], "scenarios": b["scenarios"],
+                       "setup_s": b["setup_s"], "draw": b["draw"], "l2": "inputs larger than L2",
+                       "autotune": b["autotune"]},
+            "roofline": b["roofline"], "step_roofline": b["step_roofline"], "gpu_launches": b["gpu_launches"],
+            "clocks": b["clocks"]}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
 
 
-def run_serve(args, torch):
+def measure_serve(args, torch):
     """Poisson stream (20 req/s, seed 99) of flood scenarios: rectangular cross
     or Delaunay meshes with 10k-2M triangles (log-uniform), final times
     U(60, 3600) s, mixed precision, continuous batching in one pool.  The
@@ -495,14 +620,25 @@ def run_serve(args, torch):
     summ = srv.run(reqs, realtime=True)
     clocks = sampler.stop()
     srv.close()
-    line = {"metric": METRIC, "value": summ["cell_steps_per_s"], "unit": UNIT, "n_gpus": 1,
-            "steps": summ["requests"], "warmup": 0, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
-            "config": {"workload": "serving: %d Poisson requests (20/s), 10k-2M triangles, final time 60-3600 s, "
-                       "DE1 mixed, continuous batching" % len(reqs), "mesh_setup_s": setup_s},
-            "latency": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
-                        "cell_steps": summ["cell_steps"]},
+    return {"value": summ["cell_steps_per_s"], "unit": UNIT, "requests": summ["requests"],
+            "p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
+            "cell_steps": summ["cell_steps"], "mesh_setup_s": setup_s,
+            "workload": "serving: %d Poisson requests (20/s, seed 99), rectangular cross or Delaunay, 10k-2M "
+                        "triangles, final time 60-3600 s, DE1 mixed, continuous batching in one pool, latency = "
+                        "arrival to final state on the host" % len(reqs),
             "clocks": clocks}
+
+
+def run_serve(args, torch):
+    """The serving form alone (see measure_serve)."""
+    sv = measure_serve(args, torch)
+    line = {"metric": METRIC, "value": sv["value"], "unit": UNIT, "n_gpus": 1,
+            "steps": sv["requests"], "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
+            "config": {"workload": sv["workload"], "mesh_setup_s": sv["mesh_setup_s"]},
+            "latency": {"p50_s": sv["p50_s"], "p99_s": sv["p99_s"], "wall_s": sv["wall_s"],
+                        "cell_steps": sv["cell_steps"]},
+            "clocks": sv["clocks"]}
     print(json.dumps(line))
 
 

@@ -116,6 +116,11 @@ typedef struct {
   int64_t negative_cells;      /* cumulative fix_negative_cells count */
   int32_t reason;              /* AGX_STOP_* */
   int32_t order;
+  /* cumulative time integral of the boundary flux sums, accumulated after
+   * every step as boundary_flux_integral_operator.__call__ does
+   * (operators/boundary_flux_integral_operator.py:44-62) */
+  double boundary_flux_integral;
+  int64_t nonfinite_cells;     /* cell updates that produced NaN or Inf (the loop stops on the first) */
 } agx_step_stats;
 
 #define AGX_STOP_YIELD    1
@@ -212,6 +217,11 @@ agx_status agx_divide_conserved(agx_handle h, double divisor);
 
 /* ---- device step loop ------------------------------------------------------ */
 
+/* Fixed flux timestep in place of the CFL minimum (0: variable timestepping
+ * again).  Domain.set_fixed_flux_timestep, generic_domain.py:2332-2346;
+ * applied as update_timestep does, :2358-2359. */
+agx_status agx_set_fixed_flux_timestep(agx_handle h, double flux_timestep);
+
 /* Set the evolve clock: relative time, next yield time and final time
  * (final_time < 0: none).  _evolve_base bookkeeping (generic_domain.py:1715-1826). */
 agx_status agx_set_clock(agx_handle h, double time, double yield_time, double final_time);
@@ -242,14 +252,25 @@ agx_status agx_get_stats(agx_handle h, agx_step_stats* out);
 
 /* ---- sww output (file/sww.py:260-435 store_timestep, smoothed vertices) ------- */
 /* Node -> vertex-slot map: the vertex slots 3k+i of node p are
- * node_slots[node_offsets[p] .. node_offsets[p+1]) in increasing order. */
+ * node_slots[node_offsets[p] .. node_offsets[p+1]), summed in that order
+ * (the reference's vertex_value_indices, general_mesh.py:740-850). */
 agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, const int32_t* node_slots);
 /* One output frame from the device state (vertex values as last
- * distributed): vertex_out[3P] = stage, xmomentum, ymomentum per node (mean
- * of its vertex slots, stage set to the bed where the depth is below
- * min_storable_height), centroid_out[3N] the same quantities per cell;
- * single precision, one device-to-host copy each. */
+ * distributed), as SWW_file.store_timestep forms it (file/sww.py:352-410):
+ * vertex_out[3P] = stage, xmomentum, ymomentum per node, each the mean of
+ * the node's vertex slots (quantity.c:823-870); where the mean stage minus
+ * the mean bed is below min_storable_height the stage is the bed and the
+ * momenta are zero.  centroid_out[3N] = the centroid values as they are.
+ * Single precision, one device-to-host copy each. */
 agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out);
+/* The same frame, formed and copied into a page-locked buffer of the library
+ * on the scenario's stream without waiting, so that the host can write the
+ * previous frame or issue the next yieldstep meanwhile. */
+agx_status agx_sww_frame_async(agx_handle h, double min_storable_height);
+/* Wait for the frame started last; *vertex [3P] and *centroid [3N] point
+ * into the page-locked buffer, valid until the next agx_sww_frame_async,
+ * agx_sww_bind or destroy. */
+agx_status agx_sww_frame_wait(agx_handle h, const float** vertex, const float** centroid);
 
 /* ---- diagnostics ------------------------------------------------------------- */
 int32_t agx_last_error(char* buf, int32_t n);

@@ -18,8 +18,10 @@
 extern "C" {
 #endif
 
-/* Largest mesh (triangles) the built-in scratch holds: six FP64 values per
- * edge slot, 3 slots per triangle, i.e. 9 MiB of device memory per device. */
+/* Largest mesh (triangles) the built-in scratch holds: six FP64 values and a
+ * 32-bit stamp per edge slot, 3 slots per triangle, i.e. 9.75 MiB of device
+ * memory on every device that loads the library, held until the process
+ * exits. */
 #define AGX_NOALLOC_MAX_CELLS 65536
 
 /* Device pointers, laid out as the tables of anuga_core_gb300/tables.py
@@ -27,7 +29,10 @@ extern "C" {
 typedef struct {
   int64_t N;                    /* triangles, 1 .. AGX_NOALLOC_MAX_CELLS */
   int64_t B;                    /* boundary edges */
-  int64_t E;                    /* entries of the edge list, <= 3N */
+  int64_t E;                    /* entries of the edge list, <= 3N: together the listed slots and
+                                   their opposite slots must name each of the 3N slots exactly
+                                   once (the edge list of pack_tables does); a list that misses
+                                   or repeats a slot is rejected with AGX_E_INVALID */
   const int32_t* conn;          /* [N*4] neighbours + meta word; 16-byte aligned */
   const int32_t* edge_slot;     /* [E] slot 3k+i of each listed edge */
   const int32_t* edge_opp;      /* [E] slot on the other side, -1 on the boundary */
@@ -65,6 +70,10 @@ typedef struct {
  * together) race on it and give wrong results; serialise them.  The first call
  * on each device looks up the scratch address (cudaGetSymbolAddress, which
  * may load the module); make that first call before any stream capture.
+ * With lazy module loading (the CUDA default) that first call is also when
+ * the scratch itself is committed on the device, so it needs 9.75 MiB of
+ * free device memory: make it (a warm-up call on a small mesh will do)
+ * before a host framework's caching allocator reserves the free memory.
  * Riverwalls are not applied: every edge takes the plain central flux.
  * err (may be NULL) receives a message of at most err_len bytes on failure. */
 agx_status agx_compute_fluxes_noalloc(const agx_params* params, const agx_flux_buffers* buf, int32_t substep,

@@ -36,10 +36,12 @@ int64_t agx_pool_bytes_per_cell(void);
 agx_status agx_pool_set_stream(agx_pool p, void* stream);
 
 /* Add a scenario (Domain construction, shallow_water_domain.py:231):
- * conn[N*4], geo[N*16], area[N], order[N], boundary_cell[B], lnk[N],
- * halo_off/halo_cnt per tile of 128 cells, halo_cells[n_halo]. */
+ * conn[N*4], geo[N*16], area[N], radius[N] (FP64 inscribed-circle radii,
+ * neighbour_mesh.py radii, in the stored order), order[N], boundary_cell[B],
+ * lnk[N], halo_off/halo_cnt per tile of 128 cells, halo_cells[n_halo]. */
 agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, const float* geo,
-                        const double* area, const int32_t* order, const int32_t* boundary_cell,
+                        const double* area, const double* radius, const int32_t* order,
+                        const int32_t* boundary_cell,
                         const int32_t* lnk, const int32_t* halo_off, const int32_t* halo_cnt, int64_t n_halo,
                         const int32_t* halo_cells, const agx_params* params, int32_t* sid_out);
 agx_status agx_pool_remove(agx_pool p, int32_t sid);
@@ -92,6 +94,20 @@ agx_status agx_pool_clear_operators(agx_pool p, int32_t sid);
 agx_status agx_pool_operator_influx(agx_pool p, int32_t sid, int32_t op, double* influx);
 /* distribute_to_vertices_and_edges (shallow_water_domain.py:1879-1915). */
 agx_status agx_pool_distribute(agx_pool p, int32_t sid);
+
+/* Fixed flux timestep of one scenario (0: variable timestepping again);
+ * generic_domain.py:2332-2359. */
+agx_status agx_pool_set_fixed_flux_timestep(agx_pool p, int32_t sid, double flux_timestep);
+
+/* sww frames of one scenario formed on the device (agx_sww_frame of
+ * include/agx.h: node means in the given slot order, storable-height mask
+ * at the nodes, centroid values as they are; file/sww.py:352-410).  The
+ * vertex values are those of the mixed reconstruction from the current
+ * state; slots are 3k+i in the scenario's original cell order. */
+agx_status agx_pool_sww_bind(agx_pool p, int32_t sid, int64_t P, const int32_t* node_offsets,
+                             const int32_t* node_slots);
+agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height);
+agx_status agx_pool_sww_frame_wait(agx_pool p, int32_t sid, const float** vertex, const float** centroid);
 
 /* Evolve clock of one scenario (generic_domain.py:1715-1826): relative time,
  * next yield time, final time (< 0: none), step target (0: none). */

@@ -72,10 +72,20 @@ def __getattr__(name):
 PY
 done
 cat > _shims/netCDF4.py << 'PY'
+import numpy
 import scipy.io
+from scipy.io import _netcdf
+# netCDF4 variables have a length (the record count of the first dimension)
+_netcdf.netcdf_variable.__len__ = lambda self: self.shape[0]
 class Dataset(scipy.io.netcdf_file):
     def __init__(self, filename, mode='r', format=None, **kw):
         mode = {'wl': 'w', 'w4': 'w'}.get(mode, mode)
-        super().__init__(filename, mode, version=2)
+        super().__init__(filename, mode, version=2, mmap=False)
+    def createVariable(self, name, datatype, dimensions=(), **kw):
+        # the classic format has no 64-bit integers
+        dt = numpy.dtype(datatype)
+        if dt.kind in 'iu' and dt.itemsize == 8:
+            datatype = 'i'
+        return super().createVariable(name, datatype, dimensions)
 PY
 echo "reference package built into $OUT"

@@ -144,6 +144,8 @@ def trajectory_fixture(name, build, flow_algorithm, yieldstep, finaltime):
     out["final.stage_vertex"] = Q["stage"].vertex_values.copy()
     out["yieldstep"] = np.array(yieldstep)
     out["finaltime"] = np.array(finaltime)
+    if hasattr(d, "_degenerate_calls"):
+        out["degenerate_zeroed"] = np.array(d._degenerate_calls["zeroed"])
     save(name, **out)
 
 
@@ -308,12 +310,149 @@ def flow_algorithm_fixtures():
     trajectory_fixture("traj_inflow_de1_7.npz", build_inflow_bumps, "DE1_7", 10.0, 30.0)
 
 
-if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
+def integral_fixture(name, build, flow_algorithm, yieldstep, finaltime, rain=None):
+    """Boundary flux integral, water volume and fractional-step volume at
+    every yield (shallow_water_domain.py:1630-1745, 2749-2781)."""
+    d, extra = build()
+    d.set_flow_algorithm(flow_algorithm)
+    d.set_multiprocessor_mode(2)
+    d.set_store(False)
+    out = dict(extra)
+    if rain is not None:
+        c = d.centroid_coordinates
+        L = float(c[:, 0].max())
+        idx = np.nonzero((c[:, 0] > 0.5 * L) & (c[:, 1] < 0.5 * L))[0]
+        anuga.Rate_operator(d, rate=rain, indices=idx)
+        out["rain.indices"] = idx
+        out["rain.rate"] = np.array(rain)
+    Q = d.quantities
+    out["init.stage"] = Q["stage"].centroid_values.copy()
+    out["init.xmom"] = Q["xmomentum"].centroid_values.copy()
+    out["init.ymom"] = Q["ymomentum"].centroid_values.copy()
+    out["init.elevation_c"] = Q["elevation"].centroid_values.copy()
+    out["init.friction"] = Q["friction"].centroid_values.copy()
+    v0 = d.get_water_volume()
+    times, steps, st, bfi, vol, frac = [], [], [], [], [], []
+    for t in d.evolve(yieldstep=yieldstep, finaltime=finaltime):
+        times.append(t)
+        steps.append(d.number_of_steps)
+        st.append(Q["stage"].centroid_values.copy())
+        V, BF, FS = d.report_water_volume_statistics(verbose=False, returnStats=True)
+        vol.append(V)
+        bfi.append(BF)
+        frac.append(FS)
+    out["volume0"] = np.array(v0)
+    out["times"] = np.array(times)
+    out["steps"] = np.array(steps)
+    out["stage"] = np.array(st)
+    out["boundary_flux_integral"] = np.array(bfi)
+    out["volume"] = np.array(vol)
+    out["fractional_step_volume"] = np.array(frac)
+    out["yieldstep"] = np.array(yieldstep)
+    out["finaltime"] = np.array(finaltime)
+    save(name, **out)
+
+
+def integral_fixtures():
+    # the inflow case (Dirichlet 2 m west, transmissive east): water enters
+    # and leaves through the boundaries; one stage per step (DE0), two (DE1,
+    # with rain on a quarter of the domain) and three (DE2)
+    integral_fixture("bfi_inflow_de0.npz", build_inflow_bumps, "DE0", 10.0, 30.0)
+    integral_fixture("bfi_inflow_de1_rain.npz", build_inflow_bumps, "DE1", 10.0, 30.0, rain=2.0e-4)
+    integral_fixture("bfi_inflow_de2.npz", build_inflow_bumps, "DE2", 10.0, 30.0)
+
+
+def build_inflow_fixed_dt():
+    # the inflow case with a fixed flux timestep (generic_domain.py:2332-2359)
+    d, extra = build_inflow_bumps()
+    d.set_fixed_flux_timestep(0.4)
+    extra = dict(extra)
+    extra["fixed_flux_timestep"] = np.array(0.4)
+    return d, extra
+
+
+def build_isolated_fast_cell(m=12):
+    # a lake at rest with one cell given a large momentum: its speed sits
+    # alone in the top bin of the speed histogram, so the protection against
+    # isolated degenerate timesteps (generic_domain.py:2520-2560) zeroes it
+    pts, elem, bnd = anuga.rectangular_cross(m, m, 120.0, 120.0)
+    d = anuga.Domain(pts, elem, bnd)
+    d.set_quantity("elevation", lambda x, y: -0.01 * x)
+    d.set_quantity("stage", 0.5)
+    d.set_quantity("friction", 0.02)
+    N = len(d)
+    xm = np.zeros(N)
+    xm[N // 2 + 7] = 60.0
+    d.set_quantity("xmomentum", xm, location="centroids")
+    Br = anuga.Reflective_boundary(d)
+    d.set_boundary({"left": Br, "right": Br, "top": Br, "bottom": Br})
+    d.protect_against_isolated_degenerate_timesteps = True
+    calls = {"zeroed": 0}
+    orig = d.get_quantity("xmomentum").set_values
+
+    def counting(*a, **k):
+        if k.get("indices") is not None:
+            calls["zeroed"] += 1
+        return orig(*a, **k)
+    d.get_quantity("xmomentum").set_values = counting
+    d._degenerate_calls = calls
+    return d, {"mesh.points": pts, "mesh.elements": elem, "mesh.m": np.array(m)}
+
+
+def sww_fixture(name, build, flow_algorithm, yieldstep, finaltime, minimum_storable_height):
+    """The .sww file the reference writes at every yield (file/sww.py:260-435
+    store_timestep through the netCDF stand-in), read back as arrays."""
+    import tempfile
+    from scipy.io import netcdf_file
+    d, extra = build()
+    d.set_flow_algorithm(flow_algorithm)
+    d.set_multiprocessor_mode(2)
+    out = dict(extra)
+    Q = d.quantities
+    out["init.stage"] = Q["stage"].centroid_values.copy()
+    out["init.xmom"] = Q["xmomentum"].centroid_values.copy()
+    out["init.ymom"] = Q["ymomentum"].centroid_values.copy()
+    out["init.elevation_c"] = Q["elevation"].centroid_values.copy()
+    out["init.elevation_v"] = Q["elevation"].vertex_values.copy()
+    out["init.friction"] = Q["friction"].centroid_values.copy()
+    with tempfile.TemporaryDirectory() as tmp:
+        d.set_datadir(tmp)
+        d.set_name("ref")
+        d.set_minimum_storable_height(minimum_storable_height)
+        d.set_store(True)
+        for t in d.evolve(yieldstep=yieldstep, finaltime=finaltime):
+            pass
+        f = netcdf_file(os.path.join(tmp, "ref.sww"), "r", mmap=False)
+        for k, v in f.variables.items():
+            out["sww." + k] = np.array(v[:])
+        f.close()
+    out["minimum_storable_height"] = np.array(minimum_storable_height)
+    out["yieldstep"] = np.array(yieldstep)
+    out["finaltime"] = np.array(finaltime)
+    save(name, **out)
+
+
+def option_fixtures():
+    trajectory_fixture("traj_inflow_fixed_dt_de1.npz", build_inflow_fixed_dt, "DE1", 10.0, 30.0)
+    trajectory_fixture("traj_isolated_fast_cell_de0.npz", build_isolated_fast_cell, "DE0", 0.5, 1.5)
+
+
+if __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "sww":
+    # the inflow case: partly dry, so the storable-height mask takes effect
+    sww_fixture("sww_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 30.0, 0.05)
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "options":
+    option_fixtures()
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "integrals":
+    integral_fixtures()
+elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "inlets":
     trajectory_fixture("traj_inlets_de1.npz", build_inlets, "DE1", 1.0, 6.0)
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "flows":
     flow_algorithm_fixtures()
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "boundaries":
     boundary_fixtures()
+    integral_fixtures()
+    option_fixtures()
+    sww_fixture("sww_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 30.0, 0.05)
 elif __name__ == "__main__" and len(sys.argv) > 1 and sys.argv[1] == "riverwall":
     trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)
 elif __name__ == "__main__":
@@ -330,3 +469,6 @@ elif __name__ == "__main__":
     flow_algorithm_fixtures()
     trajectory_fixture("traj_riverwall_de1.npz", build_dam_break_riverwall, "DE1", 1.0, 6.0)
     boundary_fixtures()
+    integral_fixtures()
+    option_fixtures()
+    sww_fixture("sww_inflow_de1.npz", build_inflow_bumps, "DE1", 10.0, 30.0, 0.05)

@@ -19,8 +19,9 @@ def test_pickle_round_trip_keeps_the_state(tmp_path):
     for q in ("stage", "xmomentum", "ymomentum", "elevation", "friction"):
         assert np.array_equal(d2.quantities[q].centroid_values, d.quantities[q].centroid_values)
     assert d2._scn is None and d2.get_flow_algorithm() == "DE1"
-    assert len(d2.fractional_step_operators) == 1
-    assert d2.fractional_step_operators[0].domain is d2
+    assert len(d2.fractional_step_operators) == 2      # the boundary flux integral, the rate
+    assert d2.fractional_step_operators[1].domain is d2
+    assert d2.fractional_step_operators[0] is d2.boundary_flux_integral
 
 
 def test_load_picks_the_latest_time(tmp_path):

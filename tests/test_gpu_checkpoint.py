@@ -41,6 +41,6 @@ def test_resume_continues_the_run(tmp_path, precision):
         assert np.array_equal(r.quantities["xmomentum"].centroid_values, ref.quantities["xmomentum"].centroid_values)
     else:
         assert np.abs(a - b).max() <= 1.0e-6
-    qa = r.fractional_step_operators[0].get_Q()
-    qb = ref.fractional_step_operators[0].get_Q()
+    qa = r.fractional_step_operators[1].get_Q()
+    qb = ref.fractional_step_operators[1].get_Q()
     assert abs(qa - qb) <= 1e-9 * abs(qb)

@@ -166,7 +166,7 @@ def test_rain_polygon_depth_error_within_1mm(oracle_mod):
     """The unstructured rain-and-inflow workload (random polygon, refined
     region, value-noise bed, rain patch, inflow segment) at 20k triangles."""
     d = workloads.rain_polygon(target_cells=2.0e4, precision="mixed")
-    op = d.fractional_step_operators[0]
+    op = d.fractional_step_operators[1]
     kinds = {"inflow": ("dirichlet", (3.0, 0.0, 0.0)), "wall": ("reflective", None)}
     Q = d.quantities
     st = dict(stage=Q["stage"].centroid_values.copy(), xmom=Q["xmomentum"].centroid_values.copy(),

@@ -541,29 +541,3 @@ def test_inlet_q_as_a_function_runs_on_the_device(golden):
         assert d._device_loop_ok() == (not callable_q)
         out.append(d.quantities["stage"].centroid_values.copy())
     assert np.array_equal(out[0], out[1])
-
-
-def test_sww_frames_from_the_device(tmp_path):
-    """The sww writer's device frame (storable-height mask and node means on
-    the GPU) is bitwise the frame formed on the host from the quantities, and
-    the file holds one frame per yield."""
-    from anuga_core_gb300 import workloads
-    from anuga_core_gb300.sww import read_sww
-    d = workloads.dam_break(m=20, flow_algorithm="DE1")
-    d.set_store(True)
-    d.set_datadir(str(tmp_path))
-    d.set_name("dam")
-    d.set_minimum_storable_height(0.05)
-    n = 0
-    for _ in d.evolve(yieldstep=0.5, finaltime=1.5):
-        n += 1
-        v, c = d.writer._device_frame()
-        hv, hc = d.writer.host_frame()
-        assert np.array_equal(v, hv) and np.array_equal(c, hc)
-    f = read_sww(str(tmp_path / "dam.sww"))
-    assert f["stage"].shape == (n, d.mesh.number_of_nodes) and f["stage_c"].shape == (n, len(d))
-    assert f["stage"].dtype.kind == "f" and f["stage"].dtype.itemsize == 4
-    assert np.array_equal(f["stage_c"][-1], c[0]) and np.array_equal(f["xmomentum"][-1], v[1])
-    z = d.quantities["elevation"].centroid_values.astype(np.float32)
-    dry = (d.quantities["stage"].centroid_values - d.quantities["elevation"].centroid_values) < 0.05
-    assert np.array_equal(f["stage_c"][-1][dry], z[dry])

@@ -18,6 +18,7 @@ def test_inlet_regions_match_reference(golden):
         op = agx.Inlet_operator(d, region, Q=float(f["inlet_%s.Q" % k]))
         assert np.array_equal(op.indices, np.sort(f["inlet_%s.indices" % k])), k
         assert op.area == float(np.sum(d.mesh.areas[op.indices]))
-    assert [o.device_loop for o in d.fractional_step_operators] == [True, True, True]
+    assert [o.device_loop for o in d.fractional_step_operators] == [True, True, True, True]
+    assert d.fractional_step_operators[0] is d.boundary_flux_integral
     q = agx.Inlet_operator(d, REGIONS["a"], Q=lambda t: 1.0 + t)
     assert not q.device_loop and q.update_Q(2.0) == 3.0

@@ -21,10 +21,40 @@ def test_sww_layout_and_host_frame(tmp_path):
     for q in ("stage", "xmomentum", "ymomentum"):
         assert f[q].shape == (2, P) and f[q].dtype.itemsize == 4 and f[q + "_c"].shape == (2, N)
     assert f["time"].shape == (2,)
-    zc = d.quantities["elevation"].centroid_values
-    h = d.quantities["stage"].centroid_values - zc
-    masked = h < 0.5
+    # the mask is taken at the nodes (file/sww.py:380-400): where the node's
+    # mean stage minus its mean bed is below minimum_storable_height, the
+    # stage stored is the bed and the momenta are zero; centroid values are
+    # stored as they are
+    zn = w._smooth(d.quantities["elevation"].vertex_values)
+    wn = w._smooth(d.quantities["stage"].vertex_values)
+    masked = wn - zn < 0.5
     assert masked.any() and (~masked).any()
-    assert np.array_equal(f["stage_c"][0][masked], zc[masked].astype(np.float32))
+    assert np.array_equal(f["stage"][0][masked], zn[masked].astype(np.float32))
+    assert np.array_equal(f["stage"][0][~masked], wn[~masked].astype(np.float32))
+    assert (f["xmomentum"][0][masked] == 0).all()
+    assert np.array_equal(f["stage_c"][0], d.quantities["stage"].centroid_values.astype(np.float32))
     v, c = w.host_frame()
     assert np.array_equal(f["stage"][1], v[0]) and np.array_equal(f["stage_c"][1], c[0])
+
+
+def test_node_means_follow_the_reference_summation_order():
+    """Node means add each node's vertex values one at a time in the order of
+    the mesh's vertex_value_indices and divide by the count
+    (quantity.c:823-870)."""
+    d = workloads.dam_break(m=5)
+    w = SWW_file(d)
+    rng = np.random.default_rng(3)
+    vv = rng.normal(size=(len(d), 3)) * 1e3
+    got = w._smooth(vv)
+    flat = vv.ravel()
+    vvi = np.argsort(d.mesh.triangles.ravel())
+    counts = np.bincount(d.mesh.triangles.ravel(), minlength=d.mesh.number_of_nodes)
+    want = np.zeros(d.mesh.number_of_nodes)
+    q = 0
+    for p in range(d.mesh.number_of_nodes):
+        total = 0.0
+        for _ in range(counts[p]):
+            total += flat[vvi[q]]
+            q += 1
+        want[p] = total / counts[p]
+    assert np.array_equal(got, want)

@@ -133,3 +133,57 @@ def test_noalloc_fluxes_equal_compute_fluxes(m, n, seed, alg):
             if substep == 0:
                 assert np.array_equal(out["max_speed"].cpu().numpy(), w["max_speed"]), call
             assert abs(bfs.value - w["bfs"]) <= 1e-12 * max(abs(w["bfs"]), 1e-300), (bfs.value, w["bfs"])
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_bad_edge_lists_and_recovers():
+    """An edge slot out of range, and an edge list that leaves slots
+    unwritten, are reported as AGX_E_INVALID (every load stays inside the
+    caller's arrays: the kernels check each index before using it); a valid
+    call with the same buffers right after gives the parity results."""
+    import torch
+    from anuga_core_gb300 import _lib
+    d = _case(20, 25, 12, "DE0")
+    scn = d._scn
+    T = d._tables
+    N, B = scn.N, scn.B
+    dt_ref = scn.compute_fluxes(0)
+    x_ref = scn.get("stage_x").copy()
+    dev = torch.device("cuda", 0)
+    tab = {k: torch.from_numpy(np.ascontiguousarray(T[k])).to(dev)
+           for k in ("conn", "edge_slot", "edge_opp", "normals", "edgelengths", "radii", "inv_area")}
+    out = {k: torch.zeros((N,), dtype=torch.float64, device=dev) for k in ("stage_x", "xmom_x", "ymom_x", "max_speed")}
+    E = int(T["edge_slot"].shape[0])
+
+    def buffers(edge_slot, n_edges):
+        buf = FluxBuffers()
+        buf.N, buf.B, buf.E = N, B, n_edges
+        for k, t in tab.items():
+            setattr(buf, k, t.data_ptr())
+        buf.edge_slot = edge_slot.data_ptr()
+        for k, t in out.items():
+            setattr(buf, k, t.data_ptr())
+        for k in ("stage_e", "xmom_e", "ymom_e", "elev_e", "height_e", "stage_b", "xmom_b", "ymom_b",
+                  "stage_c", "height_c", "elev_c"):
+            setattr(buf, k, scn.device_ptr(k)[0])
+        return buf
+
+    bad = tab["edge_slot"].clone()
+    bad[E // 2] = 3 * N                              # one slot index past the last slot
+    torch.cuda.synchronize()
+    f = _bind(_lib.load())
+    params = d._params()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    err = ctypes.create_string_buffer(512)
+    dt = ctypes.c_double()
+    rc = f(ctypes.byref(params), ctypes.byref(buffers(bad, E)), 0, stream, ctypes.byref(dt), None, err, 512)
+    assert rc == -1 and b"out of range" in err.value, (rc, err.value)
+    rc = f(ctypes.byref(params), ctypes.byref(buffers(tab["edge_slot"], E - 1)), 0, stream, ctypes.byref(dt), None,
+           err, 512)                                 # the last edge left out: its slots are not written
+    assert rc == -1 and b"slot results" in err.value, (rc, err.value)
+    for _ in range(2):
+        rc = f(ctypes.byref(params), ctypes.byref(buffers(tab["edge_slot"], E)), 0, stream, ctypes.byref(dt), None,
+               err, 512)
+        assert rc == 0, err.value
+        assert dt.value == dt_ref
+        assert np.array_equal(out["stage_x"].cpu().numpy(), x_ref)
