@@ -94,9 +94,9 @@ def load(path=None):
         "agx_device_ptr": ([H, ctypes.c_int32, P(ctypes.c_void_p), P(ctypes.c_int64)], ctypes.c_int32),
         "agx_set_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
         "agx_sww_bind": ([H, ctypes.c_int64, _i32p, _i32p], ctypes.c_int32),
-        "agx_sww_frame": ([H, ctypes.c_double, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
-                          ctypes.c_int32),
-        "agx_sww_frame_async": ([H, ctypes.c_double], ctypes.c_int32),
+        "agx_sww_frame": ([H, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_float),
+                           ctypes.POINTER(ctypes.c_float)], ctypes.c_int32),
+        "agx_sww_frame_async": ([H, ctypes.c_double, ctypes.c_int32], ctypes.c_int32),
         "agx_sww_frame_wait": ([H, P(ctypes.POINTER(ctypes.c_float)), P(ctypes.POINTER(ctypes.c_float))],
                                ctypes.c_int32),
         "agx_get_state": ([H, _f64p, _f64p, _f64p, ctypes.c_int64], ctypes.c_int32),
@@ -259,17 +259,18 @@ class Scenario:
         check(self.L.agx_sww_bind(self.h, off.size - 1, ptr_i32(off), ptr_i32(sl)))
         self._sww_P = off.size - 1
 
-    def sww_frame(self, min_storable_height):
+    def sww_frame(self, min_storable_height, centroid_averaging=True):
         """(vertex [3, P], centroid [3, N]) float32 output frame."""
         fp = ctypes.POINTER(ctypes.c_float)
         v = np.empty((3, self._sww_P), np.float32)
         c = np.empty((3, self.N), np.float32)
-        check(self.L.agx_sww_frame(self.h, float(min_storable_height), v.ctypes.data_as(fp), c.ctypes.data_as(fp)))
+        check(self.L.agx_sww_frame(self.h, float(min_storable_height), 1 if centroid_averaging else 0,
+                                   v.ctypes.data_as(fp), c.ctypes.data_as(fp)))
         return v, c
 
-    def sww_frame_async(self, min_storable_height):
+    def sww_frame_async(self, min_storable_height, centroid_averaging=True):
         """Start forming a frame and copying it to page-locked memory; returns at once."""
-        check(self.L.agx_sww_frame_async(self.h, float(min_storable_height)))
+        check(self.L.agx_sww_frame_async(self.h, float(min_storable_height), 1 if centroid_averaging else 0))
 
     def sww_frame_wait(self):
         """The frame started last, as copies of (vertex [3, P], centroid [3, N]) float32."""

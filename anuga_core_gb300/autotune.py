@@ -1,21 +1,32 @@
 """Autotuner for the mixed-precision pool.
 
-Two kinds of choices are made by measurement rather than fixed in code:
+Choices made by measurement rather than fixed in code:
 
-* the cell ordering (Hilbert or Morton curve) of every mesh, by the halo
-  cost of the order (extra reconstructions per tile; tables.best_order);
-* the fused flux kernel variant (register cap 80 with 3 blocks/SM, or 64 with
-  4 blocks/SM and spills) and the grid mode (persistent grid of #SMs x blocks,
-  or one block per tile), by timing a few real steps of the pool's own
-  scenarios.  The pool state is snapshotted before and restored after, so
-  tuning leaves the simulation untouched.
+* the kernel form of the step, by timing real steps of the pool's own
+  scenarios: the separate flux, update, timestep, rate and clock kernels
+  captured in the step graph with a persistent grid (at most 6 or at most 8
+  blocks of 128 threads per SM: 80 or 64 registers per thread), the same with
+  one block per tile, or the whole step as one cooperative kernel (grid
+  barriers between its phases) at either register budget;
+* whether the work records the flux kernels gather are kept resident in L2
+  (an access policy window), timed with the chosen form;
+* the cell ordering of every mesh (Hilbert or Morton curve), by the halo
+  cost of the order (extra reconstructions per tile; tables.best_order), and,
+  for a Batch, by timing steps of the pool built with each ordering
+  (batch.Batch.tune_order).
+
+The pool state is snapshotted before and restored after, so tuning leaves
+the simulation untouched.
 """
 from __future__ import annotations
 
 import time
 
-VARIANTS = [(0, 0), (0, 1), (1, 0), (1, 1)]
-NAMES = {(0, 0): "r80-persistent", (0, 1): "r80-per-tile", (1, 0): "r64-persistent", (1, 1): "r64-per-tile"}
+# (variant, grid mode): variant 0 = at most 6 blocks per SM, 1 = at most 8;
+# grid mode 0 = persistent grid, 1 = one block per tile, 2 = one-kernel step
+VARIANTS = [(0, 0), (0, 1), (1, 0), (1, 1), (0, 2), (1, 2)]
+NAMES = {(0, 0): "b6-persistent", (0, 1): "b6-per-tile", (1, 0): "b8-persistent", (1, 1): "b8-per-tile",
+         (0, 2): "b6-one-kernel", (1, 2): "b8-one-kernel"}
 
 
 def _time_steps(pool, steps, reps):
@@ -32,11 +43,13 @@ def _time_steps(pool, steps, reps):
     return best
 
 
-def tune_pool(pool, steps=10, reps=2, variants=VARIANTS):
-    """Time each kernel variant on the pool's scenarios and keep the fastest.
+def tune_pool(pool, steps=10, reps=2, variants=VARIANTS, l2=True):
+    """Time each kernel form on the pool's scenarios and keep the fastest;
+    then the same form with the work records kept in L2 (l2=True).
     Returns {name: seconds per step} and the chosen name."""
     pool.snapshot()
     res = {}
+    pool.set_l2_window(False)
     for v in variants:
         pool.set_variant(*v)
         _time_steps(pool, 1, 1)                       # build the graph once
@@ -44,5 +57,18 @@ def tune_pool(pool, steps=10, reps=2, variants=VARIANTS):
     best = min(res, key=res.get)
     v = [k for k, n in NAMES.items() if n == best][0]
     pool.set_variant(*v)
+    if l2:
+        try:
+            pool.set_l2_window(True)
+        except Exception:                             # no persisting L2 on this device
+            pool.set_l2_window(False)
+        else:
+            _time_steps(pool, 1, 1)
+            name = best + "+l2"
+            res[name] = _time_steps(pool, steps, reps) / steps
+            if res[name] < res[best]:
+                best = name
+            else:
+                pool.set_l2_window(False)
     pool.restore()
     return res, best

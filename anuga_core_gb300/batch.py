@@ -11,24 +11,69 @@ from __future__ import annotations
 import numpy as np
 
 from . import mixed
-from .tables import pack_mixed
+from .tables import hilbert_order, morton_order, pack_mixed
+
+
+ORDERS = ("per-mesh", "hilbert", "morton")
+
+
+def _tables(mesh, order):
+    """Mixed tables of a mesh in one of ORDERS: the space-filling curve with
+    the smaller halo cost for this mesh, or one curve for every mesh."""
+    if order == "per-mesh":
+        return pack_mixed(mesh)
+    C = mesh.centroid_coordinates
+    return pack_mixed(mesh, order=hilbert_order(C) if order == "hilbert" else morton_order(C))
 
 
 class Batch:
-    def __init__(self, domains, extra_cells=0, extra_scenarios=0, tables=None, distribute=False):
+    def __init__(self, domains, extra_cells=0, extra_scenarios=0, tables=None, distribute=False, order="per-mesh"):
         """distribute=True starts each scenario like evolve() does (protect
         and extrapolate first); False advances the state as it was set, like
-        Domain.advance_steps."""
+        Domain.advance_steps.  order: the cell ordering of the meshes (one of
+        ORDERS; tune_order picks it by timing)."""
         self.distribute = distribute
         self.domains = list(domains)
-        cells = sum(len(d) for d in self.domains) + int(extra_cells)
-        bnd = sum(d.mesh.boundary_length for d in self.domains) + int(extra_cells // 8 + 64)
-        ns = len(self.domains) + int(extra_scenarios)
+        self.extra = (int(extra_cells), int(extra_scenarios))
+        self.order = order
+        self.pool = self._pool(tables)
+
+    def _pool(self, tables=None):
+        cells = sum(len(d) for d in self.domains) + self.extra[0]
+        bnd = sum(d.mesh.boundary_length for d in self.domains) + int(self.extra[0] // 8 + 64)
+        ns = len(self.domains) + self.extra[1]
         self.pool = mixed.Pool(cells, max(bnd, 1), max(ns, 1))
+        if getattr(self, "_stream", None):
+            self.pool.set_stream(self._stream)
         self.sids = []
         for i, d in enumerate(self.domains):
-            T = tables[i] if tables is not None else None
+            T = tables[i] if tables is not None else _tables(d.mesh, self.order)
             self.sids.append(self._add(d, T))
+        return self.pool
+
+    def tune_order(self, steps=3, reps=2):
+        """Pick the cell ordering by timing: the pool is built with each of
+        ORDERS from the domains' states, its kernel form tuned, and a few
+        steps timed; the fastest pool is kept (in its initial state).
+        Returns ({order: seconds per step}, chosen order)."""
+        from .autotune import tune_pool
+        res, forms = {}, {}
+        for order in ORDERS:
+            if order != self.order:
+                self.pool.close()
+                self.order = order
+                self._pool()
+            times, name = tune_pool(self.pool, steps=steps, reps=reps)
+            res[order] = times[name]
+            forms[order] = (times, name)
+        best = min(res, key=res.get)
+        if best != self.order:
+            self.pool.close()
+            self.order = best
+            self._pool()
+            forms[best] = tune_pool(self.pool, steps=steps, reps=reps)
+        self.kernel_form = forms[best]          # ({form: seconds per step}, chosen form) of the kept pool
+        return res, best
 
     def _add(self, d, T=None):
         T = T if T is not None else pack_mixed(d.mesh)
@@ -59,6 +104,7 @@ class Batch:
         self.sids[i] = None
 
     def set_stream(self, ptr):
+        self._stream = ptr
         self.pool.set_stream(ptr)
 
     def advance_steps(self, n, which=None):

@@ -414,21 +414,22 @@ agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, co
   return sync(h);
 }
 
-agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out) {
+agx_status agx_sww_frame(agx_handle h, double min_storable_height, int32_t centroid_averaging, float* vertex_out,
+                         float* centroid_out) {
   AGX_TRACE("agx_sww_frame");
   if (!h || !vertex_out || !centroid_out) return fail(AGX_E_INVALID, "bad arguments");
   if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
-  CK(enqueue_sww_frame(h, h->stream, min_storable_height));
+  CK(enqueue_sww_frame(h, h->stream, min_storable_height, centroid_averaging ? 1 : 0));
   if (h->P > 0) CK(cudaMemcpyAsync(vertex_out, h->frame, (size_t)3 * h->P * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(centroid_out, h->frame + 3 * (size_t)h->P, (size_t)3 * h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   return sync(h);
 }
 
-agx_status agx_sww_frame_async(agx_handle h, double min_storable_height) {
+agx_status agx_sww_frame_async(agx_handle h, double min_storable_height, int32_t centroid_averaging) {
   AGX_TRACE("agx_sww_frame_async");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
-  CK(enqueue_sww_frame(h, h->stream, min_storable_height));
+  CK(enqueue_sww_frame(h, h->stream, min_storable_height, centroid_averaging ? 1 : 0));
   CK(cudaMemcpyAsync(h->frame_host, h->frame, ((size_t)3 * h->P + 3 * (size_t)h->N) * 4, cudaMemcpyDeviceToHost,
                      h->stream));
   CK(cudaEventRecord(h->frame_done, h->stream));

@@ -34,7 +34,7 @@ struct Clock {
 };
 
 enum ErrorBits { ERR_NUMERIC = 1, ERR_TIMESTEP = 2, ERR_OVERSHOOT = 4, ERR_NAN = 8, ERR_STEPCAP = 16,
-                 ERR_NONFINITE = 32 };
+                 ERR_NONFINITE = 32, ERR_BARRIER = 64 };
 
 // A double that is NaN or an infinity (biased exponent all ones), tested on
 // the high word with integer operations.
@@ -45,6 +45,20 @@ __host__ __device__ inline bool nonfinite64(double x) {
 }
 // hard cap on the steps one agx_advance call may take on the device
 constexpr long long MAX_STEPS_PER_CALL = 20000000;
+
+// The timestep update_timestep takes from a flux timestep, without changing
+// the clock (generic_domain.py:2349-2415): CFL scaling, the minimum timestep
+// where the small-step count runs out at first order, the clamps to the final
+// and the next yield time.  timestep_logic below applies the same steps with
+// their bookkeeping; both give the same value for the same clock.
+__host__ __device__ inline double timestep_value(const Clock* c, double flux_dt) {
+  if (c->fixed_flux_dt > 0.0) flux_dt = c->fixed_flux_dt;
+  double ts = fmin(c->cfl * flux_dt, c->max_dt);
+  if (ts < c->min_dt && c->smallsteps + 1 > c->max_smallsteps && c->order == 1) ts = c->min_dt;
+  if (c->final_time >= 0.0 && c->time + ts > c->final_time) ts = c->final_time - c->time;
+  if (c->time + ts > c->yield_time) ts = c->yield_time - c->time;
+  return ts;
+}
 
 // update_timestep (abstract_2d_finite_volumes/generic_domain.py:2349-2415):
 // CFL scaling, small-step fallback to first order, clamp to the final and the
@@ -238,7 +252,7 @@ cudaError_t enqueue_step(Scenario* s, cudaStream_t st, unsigned long long cond_h
 cudaError_t enqueue_distribute(Scenario* s, cudaStream_t st, bool with_protect, bool vertices);
 cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
 cudaError_t enqueue_op(Scenario* s, cudaStream_t st, int op, double rate, double factor, double dt);
-cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double min_storable_height);
+cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double min_storable_height, int centroid_avg);
 cudaError_t enqueue_protect(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_boundary(Scenario* s, cudaStream_t st, double t_override, bool stage2);
 cudaError_t enqueue_fluxes(Scenario* s, cudaStream_t st, int substep);

@@ -58,7 +58,7 @@ struct PoolDev {
   const int* lnk;            // per cell: staging index of each slot's neighbour (10 bits each)
   float2* tile_red1;         // [tiles] stage-1 partials: (min radius/speed, boundary flux)
   float* tile_red2;          // [tiles] stage-2 boundary flux partials
-  unsigned int* ctl;         // [2] running count and ticket of the clock kernel
+  unsigned int* ctl;         // [16] grid barrier of the one-kernel step: [0] arrivals, [1] generation, [2] timed out
   PoolScn* scn;
   const int4* conn;          // neighbours (pool-global; boundary -(m+1)) + meta
   const float4* g0;          // M00 M01 M02 M10
@@ -282,10 +282,10 @@ __device__ __forceinline__ float4 record_of(const MParams& P, double depth, doub
 // protect + preparation zeroing (distribute_to_vertices_and_edges), the
 // surrounded-by-dry zeroing, Manning friction with its semi-implicit factor
 // (sw_domain_openmp.c:1954-1986, quantity.c:772-818) and fix_negative_cells.
-// The explicit increments dt*E use the FP64 timestep of the clock (one FP64
-// fused multiply-add per quantity, so the volume applied is the one the
-// clock's time advance implies); the friction factor and its correction
-// x (q + dt E) are formed in FP32 and subtracted in FP64.
+// The depth takes dt*E with the FP64 timestep of the clock (one FP64 fused
+// multiply-add, so the volume applied is the one the clock's time advance
+// implies); the momentum increments, friction included, are formed in FP32
+// from the same timestep rounded once and added in FP64.
 // Returns 1 if the cell was fixed as negative; depth1 = w - z afterwards.
 __device__ __forceinline__ int update_lean(const MParams& P, double& depth, double& uh, double& vh,
                                            const double* area, float eta, float4 Ek, double dt, float dt32,
@@ -304,12 +304,12 @@ __device__ __forceinline__ int update_lean(const MParams& P, double& depth, doub
   const float uh32 = d2f_bits(uh), vh32 = d2f_bits(vh);
   const float x = manning_x(P, fmaxf(h, 0.0f), uh32, vh32, eta, dt32);
   depth = fma(dt, f2d_bits(Ek.x), depth);
-  uh = fma(dt, f2d_bits(Ek.y), uh);
-  vh = fma(dt, f2d_bits(Ek.z), vh);
-  if (x != 0.0f) {
-    uh = uh - f2d_bits(x * (uh32 + dt32 * Ek.y));
-    vh = vh - f2d_bits(x * (vh32 + dt32 * Ek.z));
-  }
+  float du = dt32 * Ek.y;
+  float dv = dt32 * Ek.z;
+  du = du - x * (uh32 + du);
+  dv = dv - x * (vh32 + dv);
+  uh = uh + f2d_bits(du);
+  vh = vh + f2d_bits(dv);
   if (negative_bits(depth)) {
     depth = 0.0;
     uh = 0.0;
@@ -438,10 +438,42 @@ __device__ __noinline__ float3 boundary_state_rare(int kind, const double* bv, d
 // EXT: the extended form, launched only for pools with a riverwall or a
 // boundary of kinds 7-10 (riverwall weir branch, the rarer boundaries), so
 // that the common form carries none of their registers.
-template <int STG, int MINB, bool EXT = false>
-__global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
+// Flux timestep of a scenario's step from its reduction key: the FP64
+// quotient radius / speed of the cell the key selects.
+__device__ __forceinline__ double pool_flux_dt(const PoolDev& d, const Clock& c) {
+  const unsigned long long key = c.dt_key;
+  if (!key) return 1.0e100;
+  const int cell = (int)(key & 0xffffffffull);
+  return d.radius[cell] / (double)d.maxs[cell];
+}
+
+// The timestep of the scenario's current step.  LOCALDT false: the value the
+// timestep kernel has written into the clock; true (the one-kernel step):
+// formed here from the reduction key, as the clock phase will form it.
+template <bool LOCALDT>
+__device__ __forceinline__ double step_timestep(const PoolDev& d, const PoolScn* S) {
+  if (!LOCALDT) return S->clock.timestep;
+  return timestep_value(&S->clock, pool_flux_dt(d, S->clock));
+}
+// The same for a whole warp (all lanes active): formed by lane 0 and shared,
+// so that the one-kernel step pays one FP64 division per warp and tile.
+template <bool LOCALDT>
+__device__ __forceinline__ double warp_timestep(const PoolDev& d, const PoolScn* S) {
+  if (!LOCALDT) return S->clock.timestep;
+  double v = 0.0;
+  if ((threadIdx.x & 31) == 0) v = timestep_value(&S->clock, pool_flux_dt(d, S->clock));
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+// the same in FP32 (the friction factor's timestep)
+template <bool LOCALDT>
+__device__ __forceinline__ float step_timestep32(const PoolScn* S, double ts) {
+  if (!LOCALDT) return S->clock.timestep32;
+  return (float)ts;
+}
+
+template <int STG, bool EXT, bool LOCALDT>
+__device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
   constexpr bool FUSED2 = STG >= 2;
-  __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
   const float4* W = STG == 1 ? d.W0 : (STG == 3 ? d.W2 : d.W1);
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
     const int base = tile * TILE;
@@ -459,6 +491,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
     if (STG == 2 && S->P.rk3) continue;       // RK3 scenarios take STG 4 and 3
     if (STG >= 3 && !S->P.rk3) continue;
     const MParams P = S->P;
+    const double ts_w = FUSED2 ? warp_timestep<LOCALDT>(d, S) : 0.0;     // the step's timestep
     const bool valid = k < S->cell0 + S->ncell;
     bool sdry = false;
     float4 rk = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -575,8 +608,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
             }
             case BK_TIME_SERIES: {
               double v3[3];
-              const double tnow = STG == 1 ? S->clock.time
-                                  : S->clock.time + (STG == 3 ? 0.5 : 1.0) * S->clock.timestep;
+              const double tnow = STG == 1 ? S->clock.time : S->clock.time + (STG == 3 ? 0.5 : 1.0) * ts_w;
               series_at(S->series, S->nseries, tnow, v3);
               hre = fmaxf((float)(v3[0] - d.z[k]) - L.dz, 0.0f);
               uhr = (float)v3[1];
@@ -658,7 +690,7 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
         svh = d.vhB[k];
         double h = sw, uh = suh, vh = svh;
         neg = update_lean(P, h, uh, vh, d.area + k, d.eta[k], make_float4(ew, ex, ey, sdry ? 1.f : 0.f),
-                          S->clock.timestep, S->clock.timestep32, added);
+                          ts_w, step_timestep32<LOCALDT>(S, ts_w), added);
         if (STG == 2) {
           h = half_sum(h, d.wA[k]);
           uh = half_sum(uh, d.uhA[k]);
@@ -704,10 +736,16 @@ __global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
   }
 }
 
+template <int STG, int MINB, bool EXT = false>
+__global__ void __launch_bounds__(TILE, MINB) k_pool_flux(PoolDev d) {
+  __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
+  flux_phase<STG, EXT, false>(d, es);
+}
+
 // Stage-1 update (RK2: q1 into B; Euler: in place into A) and the next
 // stage's work record.  One block per tile; warp-level bookkeeping only.
-__global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
-  (void)unused;
+template <bool LOCALDT>
+__device__ __forceinline__ void update_phase(const PoolDev& d) {
   for (int tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
     const int k = tile * TILE + threadIdx.x;
     // the cell's data are loaded before the tile's scenario is known (every
@@ -721,12 +759,13 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     if (!S->active) continue;
     const MParams P = S->P;
     const int euler = !P.rk2;
+    const double ts = warp_timestep<LOCALDT>(d, S);
     const bool valid = k < S->cell0 + S->ncell;
     int neg = 0, nf = 0;
     double added = 0.0;
     if (valid) {
-      neg = update_lean(P, h, uh, vh, d.area + k, etak, Ek, S->clock.timestep, S->clock.timestep32, added);
-      nf = nonfinite64(h) | nonfinite64(uh) | nonfinite64(vh);
+      neg = update_lean(P, h, uh, vh, d.area + k, etak, Ek, ts, step_timestep32<LOCALDT>(S, ts), added);
+      if (euler) nf = nonfinite64(h) | nonfinite64(uh) | nonfinite64(vh);   // the step's result (RK2: checked after stage 2)
       const float4 r = record_of(P, h, uh, vh);
       if (euler) {
         d.wA[k] = h; d.uhA[k] = uh; d.vhA[k] = vh;
@@ -744,9 +783,16 @@ __global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
     }
     if (nb && (threadIdx.x & 31) == 0)
       atomicAdd((unsigned long long*)&S->clock.negative_cells, (unsigned long long)__popc(nb));
-    const unsigned nfb = __ballot_sync(full, nf);
-    if (nfb && (threadIdx.x & 31) == 0) report_nonfinite(S, __popc(nfb));
+    if (euler) {                          // uniform over the tile (one scenario)
+      const unsigned nfb = __ballot_sync(full, nf);
+      if (nfb && (threadIdx.x & 31) == 0) report_nonfinite(S, __popc(nfb));
+    }
   }
+}
+
+__global__ void __launch_bounds__(TILE) k_pool_update(PoolDev d, int unused) {
+  (void)unused;
+  update_phase<false>(d);
 }
 
 // Work record from the state A (after set_field or an operator), optionally
@@ -852,10 +898,11 @@ __device__ __forceinline__ void pool_vertex(const PoolDev& d, const MParams& P, 
   vh = ve[a] + ve[b] - ve[i];
 }
 
-// sww frame of one scenario (see agx_sww_frame): node means of the vertex
-// slots, the storable-height mask at the nodes, centroid values as stored.
+// sww frame of one scenario (see agx_sww_frame): node means of the centroid
+// values of the slots' triangles (centroid_avg) or of the slots' vertex
+// values, the storable-height mask at the nodes, centroid values as stored.
 __global__ void k_pool_sww_nodes(PoolDev d, int sid, int P, const int* off, const int* slot, const int* inv,
-                                 double msh, float* out) {
+                                 double msh, int centroid_avg, float* out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const PoolScn* S = d.scn + sid;
@@ -864,8 +911,16 @@ __global__ void k_pool_sww_nodes(PoolDev d, int sid, int P, const int* off, cons
   for (int q = a; q < b; q++) {
     const int s = slot[q];
     const int ko = s / 3;
+    const int k = S->cell0 + inv[ko];
     double w, z, uh, vh;
-    pool_vertex(d, S->P, S->cell0 + inv[ko], s - 3 * ko, w, z, uh, vh);
+    if (centroid_avg) {
+      z = d.z[k];
+      w = d.wA[k] + z;
+      uh = d.uhA[k];
+      vh = d.vhA[k];
+    } else {
+      pool_vertex(d, S->P, k, s - 3 * ko, w, z, uh, vh);
+    }
     aw += w;
     az += z;
     au += uh;
@@ -1019,6 +1074,161 @@ __global__ void __launch_bounds__(INLET_TPB) k_pool_inlet(PoolDev d, PoolOp op, 
   if (threadIdx.x == 0 && slot < MAX_OPS) S->clock.op_influx[slot] += applied;
 }
 
+// ---------------------------------------------------------------------------
+// The whole DE step of every scenario in one cooperative launch (two-stage
+// and one-stage scenarios without riverwalls, the rarer boundary kinds or
+// inlets in the step loop): stage-1 fluxes, the first update, the stage-2
+// fluxes with the RK2 combine, the rates, and the clocks, separated by grid
+// barriers.  Every block computes each scenario's timestep from the reduced
+// key as the clock phase does (timestep_value), so no barrier is spent on
+// the timestep itself.
+
+// One rate operator of the one-kernel step and its influx slot.
+struct StepOp {
+  PoolOp op;
+  int slot;
+  int pad;
+};
+
+constexpr unsigned long long BARRIER_SPINS = 1ull << 26;   // with the sleeps below: tens of seconds
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier over the cooperative launch's blocks (all resident).  A
+// block whose wait runs out of spins records it in ctl[2] and returns false;
+// a block that enters with ok false does not arrive (its later barriers then
+// run out too, and the step ends with an error instead of a hang).
+__device__ bool grid_barrier(unsigned* ctl, unsigned& gen, bool ok) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int good = ok ? 1 : 0;
+    if (good) {
+      __threadfence();
+      const unsigned g = gen;
+      if (atomicAdd(&ctl[0], 1u) == gridDim.x - 1) {
+        atomicExch(&ctl[0], 0u);
+        __threadfence();
+        atomicAdd(&ctl[1], 1u);
+      } else {
+        unsigned long long n = 0;
+        while (ld_acquire_u32(&ctl[1]) == g) {
+          if (++n > BARRIER_SPINS) {
+            good = 0;
+            atomicOr(&ctl[2], 1u);
+            break;
+          }
+          __nanosleep(256);
+        }
+      }
+      gen = g + 1;
+      __threadfence();
+    }
+    s_ok = good;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Rate_operator changes of the step (k_pool_rate over the whole grid).
+__device__ void rate_phase(const PoolDev& d, const StepOp* ops, int nops) {
+  const int nthreads = gridDim.x * blockDim.x;
+  for (int o = 0; o < nops; o++) {
+    const PoolOp op = ops[o].op;
+    PoolScn* S = d.scn + op.sid;
+    if (!S->active) continue;
+    double infl = 0.0;
+    const double ts = warp_timestep<true>(d, S);         // the step's timestep, as the clock phase forms it
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < op.n; j += nthreads) {
+      const int k = op.idx[j];
+      if (op.rate >= 0.0) {
+        const double local = op.factor * ts * op.rate;
+        d.wA[k] = d.wA[k] + local;
+        infl += local * d.area[k];
+      } else {
+        const double height = d.wA[k];
+        const double local = fmax(op.factor * ts * op.rate, -height);
+        const double f = local < 0.0 ? (local + height) / (height + 1.0e-10) : 1.0;
+        d.wA[k] = d.wA[k] + local;
+        d.uhA[k] = d.uhA[k] * f;
+        d.vhA[k] = d.vhA[k] * f;
+        infl += local * d.area[k];
+      }
+      double h = d.wA[k], uh = d.uhA[k], vh = d.vhA[k], added;
+      d.W0[k] = protect_prep(S->P, h, uh, vh, d.area[k], added);
+    }
+    infl = warp_sum_d(infl);
+    if ((threadIdx.x & 31) == 0 && infl != 0.0 && ops[o].slot < MAX_OPS)
+      atomicAdd(&S->clock.op_influx[ops[o].slot], infl);
+  }
+}
+
+// The clocks (block 0): the timestep bookkeeping of k_pool_timestep, the end
+// of the step of k_pool_clock, then the accumulators of the next step are
+// cleared.  Always sets the while condition (0 after a barrier that ran out).
+__device__ void clock_phase(const PoolDev& d, int nscn, bool ok, cudaGraphConditionalHandle handle, int set_cond) {
+  int running = 0;
+  for (int s = threadIdx.x; s < nscn; s += blockDim.x) {
+    PoolScn* S = d.scn + s;
+    if (!S->alive || !S->active) continue;
+    Clock* c = &S->clock;
+    if (c->dt_key) c->dt_key = ~(unsigned long long)__double_as_longlong(pool_flux_dt(d, *c));
+    c->bfs[0] = c->bfs_acc;
+    timestep_logic(c);
+    if (!ok) c->error |= ERR_BARRIER;
+    const int reason = clock_logic(c);
+    if (reason) S->active = 0;
+    else running = 1;
+    c->dt_key = 0ull;
+    c->bfs_acc = 0.0;
+    c->bfs[1] = 0.0;
+    c->bfs[2] = 0.0;
+  }
+  const int any = __syncthreads_or(running);
+  if (threadIdx.x == 0 && set_cond) cudaGraphSetConditional(handle, (any && ok) ? 1u : 0u);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(TILE, MINB) k_pool_step(PoolDev d, const StepOp* ops, int nops, int nscn,
+                                                         cudaGraphConditionalHandle handle, int set_cond) {
+  __shared__ EdgeState es[(TILE + HALO_MAX) * 3];
+  __shared__ unsigned s_gen;
+  if (threadIdx.x == 0) s_gen = ld_acquire_u32(&d.ctl[1]);
+  __syncthreads();
+  unsigned gen = s_gen;
+  flux_phase<1, false, true>(d, es);
+  bool ok = grid_barrier(d.ctl, gen, true);
+  if (ok) update_phase<true>(d);
+  ok = grid_barrier(d.ctl, gen, ok);
+  if (ok) flux_phase<2, false, true>(d, es);
+  ok = grid_barrier(d.ctl, gen, ok);
+  if (nops > 0) {
+    if (ok) rate_phase(d, ops, nops);
+    ok = grid_barrier(d.ctl, gen, ok);
+  }
+  if (blockIdx.x == 0) clock_phase(d, nscn, ok, handle, set_cond);
+}
+
+// Before the step loop of the one-kernel step: the accumulators of the first
+// step cleared, the grid barrier's arrival count and timeout flag reset.
+__global__ void k_pool_step_prepare(PoolDev d, int nscn) {
+  for (int s = threadIdx.x; s < nscn; s += blockDim.x) {
+    Clock* c = &d.scn[s].clock;
+    c->dt_key = 0ull;
+    c->bfs_acc = 0.0;
+    c->bfs[1] = 0.0;
+    c->bfs[2] = 0.0;
+  }
+  if (threadIdx.x == 0) {
+    d.ctl[0] = 0u;
+    d.ctl[2] = 0u;
+  }
+}
+
 // Per-scenario clocks (one thread each, one block); sets the graph's while
 // condition when any scenario is still running.
 __global__ void k_pool_clock(PoolDev d, int nscn, cudaGraphConditionalHandle handle, int set_cond) {
@@ -1126,8 +1336,15 @@ struct Pool {
   bool graph_valid = false;
   int grid = 0;
   int grid_v[2] = {0, 0};        // persistent grid per flux variant
-  int variant = 0;               // flux kernel variant: 0 = 80 registers (3 blocks/SM), 1 = 64 registers
-  int grid_mode = 0;             // 0 = persistent grid, 1 = one block per tile
+  int variant = 1;               // flux kernel variant: 0 = at most 6 blocks of 128 per SM (80 registers),
+                                 // 1 = at most 8 (64 registers; the faster one on every large pool measured)
+  int grid_mode = 0;             // 0 = persistent grid, 1 = one block per tile, 2 = one-kernel step
+  int step_grid[2] = {0, 0};     // resident blocks of the one-kernel step per variant
+  StepOp* step_ops = nullptr;    // device table of the step loop's rate operators
+  int step_nops = 0;
+  int l2_window = 0;             // 1: the work records a kernel gathers are kept in L2 (access policy window)
+  size_t l2_persist_max = 0;     // the device's persisting L2 size and window limit
+  size_t l2_window_max = 0;
   void* snap = nullptr;          // snapshot of the dynamic state (autotuning, checkpoints)
   size_t snap_bytes = 0;
   int kernels_per_iter = 0;
@@ -1280,18 +1497,40 @@ static int nblk1(int n) { return (n + 255) / 256; }
 // One step of every active scenario in two parts: the first stage (flux,
 // timestep, first update; Euler scenarios are complete after it), then the
 // second RK2 stage, the operators of the step loop and the clocks.
+// With the pool's L2 option on, the kernels launched next on `st` keep the
+// work records `rec` of the used cells resident in L2 (persisting accesses
+// up to the device's persisting size; the rest stream).  rec null: no window.
+// Kernels captured into the step graph take the stream's window with them.
+static void set_l2_window(Pool* p, cudaStream_t st, const void* rec) {
+  if (!p->l2_window && rec) return;
+  cudaStreamAttrValue v = {};
+  if (rec && p->l2_window_max > 0) {
+    const size_t bytes = std::min((size_t)p->d.ntiles * TILE * 16, p->l2_window_max);
+    v.accessPolicyWindow.base_ptr = const_cast<void*>(rec);
+    v.accessPolicyWindow.num_bytes = bytes;
+    v.accessPolicyWindow.hitRatio = bytes ? (float)std::min(1.0, (double)p->l2_persist_max / (double)bytes) : 0.0f;
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  } else {
+    v.accessPolicyWindow.num_bytes = 0;
+  }
+  cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &v);
+}
+
 static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   const PoolDev& d = p->d;
   p->scn_fresh = false;
   const int S = p->cap_scn;
   k_pool_reset<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
-  const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
+  const int Gf = p->grid_mode == 1 ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
+  set_l2_window(p, st, d.W0);
   if (p->rw_any || p->rare_bc_any) k_pool_flux<1, 6, true><<<Gf, TILE, 0, st>>>(d);
   else if (p->variant == 0) k_pool_flux<1, 6><<<Gf, TILE, 0, st>>>(d);
   else k_pool_flux<1, 8><<<Gf, TILE, 0, st>>>(d);
   count_launch();
   phase_mark(st, PH_FLUX);
+  set_l2_window(p, st, d.W1);        // the update writes the records stage 2 gathers
   k_pool_timestep<<<nblk1(S), 256, 0, st>>>(d, S);
   count_launch();
   phase_mark(st, PH_SMALL);
@@ -1301,6 +1540,7 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
   k_pool_update<<<std::max(d.ntiles, 1), TILE, 0, st>>>(d, 0);
   count_launch();
   phase_mark(st, PH_UPDATE);
+  if (p->l2_window) set_l2_window(p, st, nullptr);
   return cudaGetLastError();
 }
 
@@ -1308,8 +1548,9 @@ static cudaError_t enqueue_first_stage(Pool* p, cudaStream_t st) {
 static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
   const PoolDev& d = p->d;
   p->scn_fresh = false;
-  const int Gf = p->grid_mode ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
+  const int Gf = p->grid_mode == 1 ? std::max(d.ntiles, 1) : p->grid_v[p->variant];
   if (stage == 3 && !p->rk3_any) return cudaSuccess;
+  set_l2_window(p, st, stage == 3 ? (const void*)d.W2 : (const void*)d.W1);
   if (stage == 2) {
     if (p->rw_any || p->rare_bc_any) k_pool_flux<2, 6, true><<<Gf, TILE, 0, st>>>(d);
     else if (p->variant == 0) k_pool_flux<2, 6><<<Gf, TILE, 0, st>>>(d);
@@ -1327,6 +1568,7 @@ static cudaError_t enqueue_later_stage(Pool* p, cudaStream_t st, int stage) {
   }
   count_launch();
   phase_mark(st, PH_FLUX);
+  if (p->l2_window) set_l2_window(p, st, nullptr);
   return cudaGetLastError();
 }
 
@@ -1352,7 +1594,59 @@ static cudaError_t enqueue_step_end(Pool* p, cudaStream_t st, unsigned long long
   return cudaGetLastError();
 }
 
+// The one-kernel step serves pools whose scenarios take one or two stages,
+// without riverwalls, boundary kinds 7-10 or inlets in the step loop.
+static bool step_kernel_ok(const Pool* p) {
+  if (p->rk3_any || p->rw_any || p->rare_bc_any) return false;
+  for (const ScnHost& sh : p->scn) {
+    if (!sh.alive || sh.host_ops) continue;
+    for (const PoolOp& op : sh.ops) if (op.kind != 0) return false;
+  }
+  return true;
+}
+
+// Device table of the step loop's rate operators (rebuilt with the graph).
+static agx_status build_step_ops(Pool* p) {
+  std::vector<StepOp> v;
+  for (size_t s = 0; s < p->scn.size(); s++) {
+    const ScnHost& sh = p->scn[s];
+    if (!sh.alive || sh.host_ops) continue;
+    for (size_t i = 0; i < sh.ops.size(); i++) v.push_back(StepOp{sh.ops[i], (int)i, 0});
+  }
+  if (p->step_ops) cudaFree(p->step_ops);
+  p->step_ops = nullptr;
+  p->step_nops = (int)v.size();
+  if (v.empty()) return AGX_OK;
+  PCK(cudaMalloc(&p->step_ops, v.size() * sizeof(StepOp)));
+  PCK(cudaMemcpyAsync(p->step_ops, v.data(), v.size() * sizeof(StepOp), cudaMemcpyHostToDevice, p->stream));
+  return psync(p);
+}
+
+static cudaError_t enqueue_step_kernel(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  p->scn_fresh = false;
+  const int G = std::max(1, std::min(p->step_grid[p->variant], std::max(p->d.ntiles, 1)));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(TILE);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const StepOp* ops = p->step_ops;
+  const int nops = p->step_nops, nscn = p->cap_scn, sc = set_cond ? 1 : 0;
+  const cudaGraphConditionalHandle hh = (cudaGraphConditionalHandle)h;
+  cudaError_t e = p->variant == 0 ? cudaLaunchKernelEx(&cfg, k_pool_step<6>, p->d, ops, nops, nscn, hh, sc)
+                                  : cudaLaunchKernelEx(&cfg, k_pool_step<8>, p->d, ops, nops, nscn, hh, sc);
+  count_launch();
+  phase_mark(st, PH_FLUX);
+  return e;
+}
+
 static cudaError_t enqueue_pool_iter(Pool* p, cudaStream_t st, unsigned long long h, bool set_cond) {
+  if (p->grid_mode == 2 && step_kernel_ok(p) && set_cond) return enqueue_step_kernel(p, st, h, set_cond);
   cudaError_t e = enqueue_first_stage(p, st);
   if (e == cudaSuccess) e = enqueue_later_stage(p, st, 2);
   if (e == cudaSuccess) e = enqueue_later_stage(p, st, 3);
@@ -1368,12 +1662,29 @@ static agx_status pool_build_graph(Pool* p) {
   PCK(cudaGraphCreate(&p->graph, 0));
   cudaGraphConditionalHandle handle;
   PCK(cudaGraphConditionalHandleCreate(&handle, p->graph, 1, cudaGraphCondAssignDefault));
+  const bool one_kernel = p->grid_mode == 2 && step_kernel_ok(p);
+  cudaGraphNode_t prep = nullptr;
+  if (one_kernel) {
+    agx_status so = build_step_ops(p);
+    if (so) return so;
+    // accumulators and barrier words cleared once before the loop
+    PoolDev dev = p->d;
+    int nscn = p->cap_scn;
+    void* args[] = {&dev, &nscn};
+    cudaKernelNodeParams kp = {};
+    kp.func = (void*)k_pool_step_prepare;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(256);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    PCK(cudaGraphAddKernelNode(&prep, p->graph, nullptr, 0, &kp));
+  }
   cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
   np.conditional.handle = handle;
   np.conditional.type = cudaGraphCondTypeWhile;
   np.conditional.size = 1;
   cudaGraphNode_t node;
-  PCK(cudaGraphAddNode(&node, p->graph, nullptr, nullptr, 0, &np));
+  PCK(cudaGraphAddNode(&node, p->graph, prep ? &prep : nullptr, nullptr, prep ? 1 : 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
   PCK(cudaStreamSynchronize(p->stream));
   PCK(cudaStreamBeginCaptureToGraph(p->own_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
@@ -1435,6 +1746,11 @@ agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
   p->grid = std::max(1, sms * std::max(per, 1));
   p->grid_v[0] = p->grid;
   p->grid_v[1] = std::max(1, sms * std::max(per4, 1));
+  int ps6 = 0, ps8 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps6, k_pool_step<6>, TILE, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps8, k_pool_step<8>, TILE, 0);
+  p->step_grid[0] = sms * std::max(ps6, 0);
+  p->step_grid[1] = sms * std::max(ps8, 0);
   *out = p;
   return AGX_OK;
 }
@@ -1470,6 +1786,7 @@ agx_status agx_pool_destroy(agx_pool p) {
   if (p->snap) cudaFree(p->snap);
   if (p->rw_mem) cudaFree(p->rw_mem);
   if (p->w2_mem) cudaFree(p->w2_mem);
+  if (p->step_ops) cudaFree(p->step_ops);
   if (p->rw_hyd_dev) cudaFree(p->rw_hyd_dev);
   if (p->scn_host) cudaFreeHost(p->scn_host);
   if (p->own_stream) cudaStreamDestroy(p->own_stream);
@@ -2287,7 +2604,7 @@ agx_status agx_pool_sww_bind(agx_pool p, int32_t sid, int64_t P, const int32_t* 
   return psync(p);
 }
 
-agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height) {
+agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height, int32_t centroid_averaging) {
   AGX_TRACE("agx_pool_sww_frame_async");
   if (!p || sid < 0 || sid >= p->cap_scn || !p->scn[sid].alive) return pfail(AGX_E_INVALID, "bad scenario");
   ScnHost& sh = p->scn[sid];
@@ -2297,7 +2614,7 @@ agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable
   cudaStream_t s = p->stream;
   if (sh.sww_P > 0) {
     k_pool_sww_nodes<<<nblk1(sh.sww_P), 256, 0, s>>>(p->d, sid, sh.sww_P, sh.sww_off, sh.sww_slot, sh.inv,
-                                                    min_storable_height, sh.frame);
+                                                    min_storable_height, centroid_averaging ? 1 : 0, sh.frame);
     count_launch();
   }
   k_pool_sww_cells<<<nblk1(sh.N), 256, 0, s>>>(p->d, sid, sh.order, sh.frame + 3 * (size_t)sh.sww_P);
@@ -2335,6 +2652,9 @@ agx_status agx_pool_get_stats(agx_pool p, int32_t sid, agx_step_stats* out) {
   if (st) return st;
   fill_stats_p(&p->scn_host[sid].clock, out);
   const int e = p->scn_host[sid].clock.error;
+  if (e & ERR_BARRIER)
+    return pfail(AGX_E_TIMEOUT, "a grid barrier of the one-kernel step ran out of waiting; the step loop of scenario "
+                 "%d stopped", sid);
   if (e & ERR_NONFINITE)
     return pfail(AGX_E_NUMERIC, "non-finite conserved quantity (NaN or Inf) in %lld cell updates of scenario %d; "
                  "its step loop stopped", (long long)p->scn_host[sid].clock.nonfinite_cells, sid);
@@ -2396,6 +2716,28 @@ agx_status agx_pool_time_phases(agx_pool p, int32_t reps, double* ms, int32_t n_
 }
 
 int32_t agx_pool_grid(agx_pool p) { return p ? p->grid : 0; }
+
+// Keep the work records the flux kernels gather resident in L2 (1) or not
+// (0).  The first time it is switched on, the context's persisting L2 size is
+// set to the device's maximum (a limit of this process's context only).
+agx_status agx_pool_set_l2_window(agx_pool p, int32_t on) {
+  if (!p) return pfail(AGX_E_INVALID, "null pool");
+  agx_status st = psync(p);
+  if (st) return st;
+  if (on && p->l2_window_max == 0) {
+    int persist = 0, window = 0;
+    PCK(cudaDeviceGetAttribute(&persist, cudaDevAttrMaxPersistingL2CacheSize, p->device));
+    PCK(cudaDeviceGetAttribute(&window, cudaDevAttrMaxAccessPolicyWindowSize, p->device));
+    if (persist <= 0 || window <= 0) return pfail(AGX_E_STATE, "this device has no persisting L2");
+    PCK(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)persist));
+    p->l2_persist_max = (size_t)persist;
+    p->l2_window_max = (size_t)window;
+  }
+  if ((on != 0) != (p->l2_window != 0)) p->graph_valid = false;
+  p->l2_window = on ? 1 : 0;
+  if (!on) set_l2_window(p, p->stream, nullptr);
+  return AGX_OK;
+}
 
 // Continuous batching: give every running scenario up to max_steps more
 // steps (stopping early at its final or yield time) and launch the device
@@ -2479,11 +2821,12 @@ agx_status agx_pool_capacity(agx_pool p, int64_t* free_cells, int64_t* free_boun
   return AGX_OK;
 }
 
-// Kernel variant of the fused flux kernels (0: 80 registers, 3 blocks/SM;
-// 1: 64 registers, 4 blocks/SM) and grid mode (0: persistent, 1: one block
-// per tile).  Chosen by the autotuner.
+// Kernel variant of the fused flux kernels (0: at most 6 blocks of 128 per
+// SM, 1: at most 8) and grid mode (0: persistent, 1: one block per tile, 2:
+// the whole step in one cooperative kernel where the pool allows it).
+// Chosen by the autotuner.
 agx_status agx_pool_set_variant(agx_pool p, int32_t variant, int32_t grid_mode) {
-  if (!p || variant < 0 || variant > 1 || grid_mode < 0 || grid_mode > 1) return pfail(AGX_E_INVALID, "bad variant");
+  if (!p || variant < 0 || variant > 1 || grid_mode < 0 || grid_mode > 2) return pfail(AGX_E_INVALID, "bad variant");
   if (p->variant != variant || p->grid_mode != grid_mode) p->graph_valid = false;
   p->variant = variant;
   p->grid_mode = grid_mode;

@@ -408,24 +408,34 @@ __global__ void __launch_bounds__(INLET_TPB) k_inlet(Dev d, RateOp op, int slot,
   if (threadIdx.x == 0 && slot < MAX_OPS) d.clock->op_influx[slot] += applied;
 }
 
-// One sww frame (file/sww.py:352-410 store_timestep with smoothed vertex
-// values): per node the mean of its vertex slots in the order the caller
-// gives (the reference's vertex_value_indices, summed as
-// quantity.c:823-870 _average_vertex_values does, total / k); a node is
+// One sww frame (file/sww.py:352-410 store_timestep, smoothed node values):
+// per node the mean over its vertex slots in the order the caller gives (the
+// reference's vertex_value_indices, summed and divided as quantity.c:823-915
+// do, total / k) of the centroid values of the slots' triangles
+// (centroid_avg: the DE algorithms' centroid averaging,
+// shallow_water_domain.py:596) or of the slots' vertex values; a node is
 // storable when its mean stage minus its mean bed is at least
 // minimum_storable_height: otherwise the stage stored is the bed and the
 // momenta are zero.  Centroid values are stored as they are.  All as float.
-__global__ void k_sww_nodes(Dev d, int P, const int* off, const int* slot, double msh, float* out) {
+__global__ void k_sww_nodes(Dev d, int P, const int* off, const int* slot, double msh, int centroid_avg, float* out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   double aw = 0.0, az = 0.0, au = 0.0, av = 0.0;
   const int a = off[p], b = off[p + 1];
   for (int q = a; q < b; q++) {
     const int s = slot[q];
-    aw += d.wv[s];
-    az += d.zv[s];
-    au += d.uhv[s];
-    av += d.vhv[s];
+    if (centroid_avg) {
+      const int k = s / 3;
+      aw += d.w[k];
+      az += d.z[k];
+      au += d.uh[k];
+      av += d.vh[k];
+    } else {
+      aw += d.wv[s];
+      az += d.zv[s];
+      au += d.uhv[s];
+      av += d.vhv[s];
+    }
   }
   if (b > a) {
     const double k = (double)(b - a);
@@ -618,9 +628,10 @@ cudaError_t enqueue_rate_once(Scenario* s, cudaStream_t st, int i, double rate, 
   return cudaSuccess;
 }
 
-cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double msh) {
+cudaError_t enqueue_sww_frame(Scenario* s, cudaStream_t st, double msh, int centroid_avg) {
   const Dev& d = s->d;
-  if (s->P > 0) LAUNCH(k_sww_nodes<<<nblk(s->P), TPB, 0, st>>>(d, s->P, s->node_off, s->node_slot, msh, s->frame));
+  if (s->P > 0)
+    LAUNCH(k_sww_nodes<<<nblk(s->P), TPB, 0, st>>>(d, s->P, s->node_off, s->node_slot, msh, centroid_avg, s->frame));
   if (d.N > 0) LAUNCH(k_sww_cells<<<nblk(d.N), TPB, 0, st>>>(d, s->frame + 3 * (size_t)s->P));
   return cudaSuccess;
 }

@@ -224,7 +224,18 @@ class Domain:
             setattr(self, k, d[k])
         self.default_order = 2
         self._order_ = 2
+        # the DE algorithms store node values as means of centroid values
+        # (shallow_water_domain.py:596, 659, 722)
+        self.using_centroid_averaging = True
         self._invalidate_device()
+
+    def set_using_centroid_averaging(self, flag=True):
+        """Node values (sww output) as means of the adjacent centroid values
+        (True) or of the vertex values (False); generic_domain.py:765-782."""
+        self.using_centroid_averaging = bool(flag)
+
+    def get_using_centroid_averaging(self):
+        return self.using_centroid_averaging
 
     def get_flow_algorithm(self):
         return self.flow_algorithm

@@ -56,7 +56,7 @@ def lib():
             "agx_pool_distribute": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_set_fixed_flux_timestep": ([H, ctypes.c_int32, ctypes.c_double], ctypes.c_int32),
             "agx_pool_sww_bind": ([H, ctypes.c_int32, ctypes.c_int64, _i32p, _i32p], ctypes.c_int32),
-            "agx_pool_sww_frame_async": ([H, ctypes.c_int32, ctypes.c_double], ctypes.c_int32),
+            "agx_pool_sww_frame_async": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_sww_frame_wait": ([H, ctypes.c_int32, P(ctypes.POINTER(ctypes.c_float)),
                                          P(ctypes.POINTER(ctypes.c_float))], ctypes.c_int32),
             "agx_pool_set_clock": ([H, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -71,6 +71,7 @@ def lib():
             "agx_pool_time_phases": ([H, ctypes.c_int32, _f64p, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_grid": ([H], ctypes.c_int32),
             "agx_pool_set_variant": ([H, ctypes.c_int32, ctypes.c_int32], ctypes.c_int32),
+            "agx_pool_set_l2_window": ([H, ctypes.c_int32], ctypes.c_int32),
             "agx_pool_snapshot": ([H], ctypes.c_int32),
             "agx_pool_launch_chunk": ([H, ctypes.c_int64], ctypes.c_int32),
             "agx_pool_wait": ([H, P(ctypes.c_int32)], ctypes.c_int32),
@@ -230,8 +231,9 @@ class Pool:
         check(self.L.agx_pool_sww_bind(self.h, int(sid), off.size - 1, off.ctypes.data_as(_i32p),
                                        sl.ctypes.data_as(_i32p)))
 
-    def sww_frame_async(self, sid, min_storable_height):
-        check(self.L.agx_pool_sww_frame_async(self.h, int(sid), float(min_storable_height)))
+    def sww_frame_async(self, sid, min_storable_height, centroid_averaging=True):
+        check(self.L.agx_pool_sww_frame_async(self.h, int(sid), float(min_storable_height),
+                                              1 if centroid_averaging else 0))
 
     def sww_frame_wait(self, sid, P):
         N, _ = self._keep[sid]
@@ -287,6 +289,10 @@ class Pool:
     def set_variant(self, variant, grid_mode):
         check(self.L.agx_pool_set_variant(self.h, int(variant), int(grid_mode)))
         self.variant = (int(variant), int(grid_mode))
+
+    def set_l2_window(self, on):
+        check(self.L.agx_pool_set_l2_window(self.h, 1 if on else 0))
+        self.l2_window = bool(on)
 
     def snapshot(self):
         check(self.L.agx_pool_snapshot(self.h))
@@ -445,14 +451,14 @@ class MixedScenario:
         self.pool.sww_bind(self.sid, node_offsets, node_slots)
         self._sww_P = len(node_offsets) - 1
 
-    def sww_frame_async(self, min_storable_height):
-        self.pool.sww_frame_async(self.sid, min_storable_height)
+    def sww_frame_async(self, min_storable_height, centroid_averaging=True):
+        self.pool.sww_frame_async(self.sid, min_storable_height, centroid_averaging)
 
     def sww_frame_wait(self):
         return self.pool.sww_frame_wait(self.sid, self._sww_P)
 
-    def sww_frame(self, min_storable_height):
-        self.sww_frame_async(min_storable_height)
+    def sww_frame(self, min_storable_height, centroid_averaging=True):
+        self.sww_frame_async(min_storable_height, centroid_averaging)
         return self.sww_frame_wait()
 
     def set_stream(self, ptr):

@@ -5,10 +5,13 @@ dimensions number_of_volumes / number_of_vertices / number_of_points /
 number_of_timesteps; variables x, y, volumes, time, elevation, friction,
 stage, xmomentum, ymomentum in single precision, their ``*_range`` and the
 ``*_c`` centroid variables).  A frame is formed as SWW_file.store_timestep
-does (file/sww.py:352-410): per node the mean of its vertex values, summed in
+does (file/sww.py:352-410): per node the mean over its vertex slots, summed in
 the order of the mesh's vertex_value_indices (general_mesh.py:830, the
-default numpy argsort of the triangles; quantity.c:823-870 divides the sum by
-the count); where the mean stage minus the mean bed is below
+default numpy argsort of the triangles) and divided by their count, of the
+centroid values of the slots' triangles (the centroid averaging that every
+DE flow algorithm switches on, shallow_water_domain.py:596; quantity.c:872-915)
+or, with centroid averaging off, of the slots' vertex values
+(quantity.c:823-870); where the mean stage minus the mean bed is below
 minimum_storable_height the node's stage is its bed and its momenta are zero;
 centroid values are stored as they are.
 
@@ -81,14 +84,19 @@ class SWW_file:
         if scn is None:
             return None
         self.flush()
-        scn.sww_frame_async(self.domain.minimum_storable_height)
+        d = self.domain
+        scn.sww_frame_async(d.minimum_storable_height, d.get_using_centroid_averaging())
         return scn.sww_frame_wait()
 
-    def _smooth(self, vertex_values):
-        """Node means of vertex values as quantity.c:823-870 forms them: the
-        node's vertex values added one at a time in vertex_value_indices
-        order, the total divided by their count."""
-        v = np.asarray(vertex_values, float).ravel()[self._vvi]
+    def _smooth(self, vertex_values, centroid_values=None):
+        """Node means as quantity.c:823-915 forms them: the values of the
+        node's vertex slots (the centroid value of the slot's triangle when
+        centroid_values is given, else the slot's vertex value) added one at a
+        time in vertex_value_indices order, the total divided by the count."""
+        if centroid_values is not None:
+            v = np.asarray(centroid_values, float)[self._vvi // 3]
+        else:
+            v = np.asarray(vertex_values, float).ravel()[self._vvi]
         acc = np.zeros(self.P)
         start = self._off[:-1]
         for j in range(int(self._counts.max()) if self.P else 0):
@@ -98,16 +106,22 @@ class SWW_file:
         acc[nz] = acc[nz] / self._counts[nz]
         return acc
 
+    def _node_values(self, q):
+        Q = self.domain.quantities[q]
+        if self.domain.get_using_centroid_averaging():
+            return self._smooth(None, Q.centroid_values)
+        return self._smooth(Q.vertex_values)
+
     def host_frame(self):
         """The same frame formed on the host from the quantities."""
         d = self.domain
         Q = d.quantities
-        wn = self._smooth(Q["stage"].vertex_values)
-        zn = self._smooth(Q["elevation"].vertex_values)
+        wn = self._node_values("stage")
+        zn = self._node_values("elevation")
         storable = wn - zn >= d.minimum_storable_height
         V = [np.where(storable, wn.astype(np.float32), zn.astype(np.float32)).astype(np.float32)]
         for q in ("xmomentum", "ymomentum"):
-            A = self._smooth(Q[q].vertex_values).astype(np.float32)
+            A = self._node_values(q).astype(np.float32)
             V.append(np.where(storable, A, np.float32(0.0)).astype(np.float32))
         C = [Q[q].centroid_values.astype(np.float32) for q in DYNAMIC]
         return np.array(V), np.array(C)
@@ -133,7 +147,7 @@ class SWW_file:
         f.createVariable("time", "d", ("number_of_timesteps",))
         for q in STATIC:
             v = f.createVariable(q, "f", ("number_of_points",))
-            A = self._smooth(d.quantities[q].vertex_values).astype(np.float32)
+            A = self._node_values(q).astype(np.float32)
             v[:] = A
             r = f.createVariable(q + "_range", "f", ("numbers_in_range",))
             r[:] = np.array([A.min(), A.max()], np.float32) if A.size else np.zeros(2, np.float32)
@@ -178,7 +192,7 @@ class SWW_file:
             V, C = self.host_frame()
             self._append(t, V, C)
             return
-        scn.sww_frame_async(d.minimum_storable_height)
+        scn.sww_frame_async(d.minimum_storable_height, d.get_using_centroid_averaging())
         if self.asynchronous:
             if self._exec is None:
                 self._exec = concurrent.futures.ThreadPoolExecutor(max_workers=1)

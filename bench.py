@@ -500,8 +500,8 @@ def measure_batch(args, torch, world, dist, steps, err_sample=0):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     B.set_stream(stream.cuda_stream)
-    from anuga_core_gb300.autotune import tune_pool
-    res, best = tune_pool(B.pool, steps=3, reps=2)
+    order_s, order = B.tune_order(steps=3, reps=2)
+    res, best = B.kernel_form
     B.advance_steps(args.warmup)
     launches0 = _lib.kernel_launches()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -527,7 +527,8 @@ def measure_batch(args, torch, world, dist, steps, err_sample=0):
     out = {"value": value, "unit": UNIT, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
            "workload": "batch of %d rectangular-cross scenarios, sides log-uniform [20,400], %d triangles, "
                        "DE1 mixed, one pool" % (len(doms), N), "cells": N, "scenarios": len(doms),
-           "setup_s": setup_s, "draw": info["draw"], "autotune": {"chosen": best, "s_per_step": res},
+           "setup_s": setup_s, "draw": info["draw"],
+           "autotune": {"chosen": best, "s_per_step": res, "order": order, "order_s_per_step": order_s},
            "roofline": {"bound": "hbm", "achieved": ach_k, "peak": hbm, "unit": "GB/s",
                         "frac": ach_k / hbm if ach_k else None, "peak_kind": peak_kind,
                         "traffic": tr["bytes_per_cell"] * N if tr else None,
@@ -614,7 +615,7 @@ def measure_serve(args, torch):
     for r in reqs:                 # build the meshes of the stream up front (mesh cache warm)
         cache.get(r.kind, r.cells)
     setup_s = time.time() - t0
-    srv = FloodServer(max_scenarios=256, chunk_steps=64, mesh_cache=cache)
+    srv = FloodServer(max_scenarios=256, chunk_steps=128, mesh_cache=cache)
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
     summ = srv.run(reqs, realtime=True)

@@ -255,18 +255,21 @@ agx_status agx_get_stats(agx_handle h, agx_step_stats* out);
  * node_slots[node_offsets[p] .. node_offsets[p+1]), summed in that order
  * (the reference's vertex_value_indices, general_mesh.py:740-850). */
 agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, const int32_t* node_slots);
-/* One output frame from the device state (vertex values as last
- * distributed), as SWW_file.store_timestep forms it (file/sww.py:352-410):
- * vertex_out[3P] = stage, xmomentum, ymomentum per node, each the mean of
- * the node's vertex slots (quantity.c:823-870); where the mean stage minus
- * the mean bed is below min_storable_height the stage is the bed and the
- * momenta are zero.  centroid_out[3N] = the centroid values as they are.
- * Single precision, one device-to-host copy each. */
-agx_status agx_sww_frame(agx_handle h, double min_storable_height, float* vertex_out, float* centroid_out);
+/* One output frame from the device state, as SWW_file.store_timestep forms
+ * it (file/sww.py:352-410): vertex_out[3P] = stage, xmomentum, ymomentum per
+ * node, each the mean over the node's vertex slots of the centroid values of
+ * their triangles (centroid_averaging = 1, what the DE algorithms set,
+ * shallow_water_domain.py:596; quantity.c:872-915) or of the slots' vertex
+ * values as last distributed (0; quantity.c:823-870); where the mean stage
+ * minus the mean bed is below min_storable_height the stage is the bed and
+ * the momenta are zero.  centroid_out[3N] = the centroid values as they
+ * are.  Single precision, one device-to-host copy each. */
+agx_status agx_sww_frame(agx_handle h, double min_storable_height, int32_t centroid_averaging, float* vertex_out,
+                         float* centroid_out);
 /* The same frame, formed and copied into a page-locked buffer of the library
  * on the scenario's stream without waiting, so that the host can write the
  * previous frame or issue the next yieldstep meanwhile. */
-agx_status agx_sww_frame_async(agx_handle h, double min_storable_height);
+agx_status agx_sww_frame_async(agx_handle h, double min_storable_height, int32_t centroid_averaging);
 /* Wait for the frame started last; *vertex [3P] and *centroid [3N] point
  * into the page-locked buffer, valid until the next agx_sww_frame_async,
  * agx_sww_bind or destroy. */

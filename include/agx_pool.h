@@ -100,13 +100,13 @@ agx_status agx_pool_distribute(agx_pool p, int32_t sid);
 agx_status agx_pool_set_fixed_flux_timestep(agx_pool p, int32_t sid, double flux_timestep);
 
 /* sww frames of one scenario formed on the device (agx_sww_frame of
- * include/agx.h: node means in the given slot order, storable-height mask
- * at the nodes, centroid values as they are; file/sww.py:352-410).  The
- * vertex values are those of the mixed reconstruction from the current
- * state; slots are 3k+i in the scenario's original cell order. */
+ * include/agx.h: node means of centroid or vertex values in the given slot
+ * order, storable-height mask at the nodes, centroid values as they are;
+ * file/sww.py:352-410).  Vertex values are those of the mixed reconstruction
+ * from the current state; slots are 3k+i in the original cell order. */
 agx_status agx_pool_sww_bind(agx_pool p, int32_t sid, int64_t P, const int32_t* node_offsets,
                              const int32_t* node_slots);
-agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height);
+agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable_height, int32_t centroid_averaging);
 agx_status agx_pool_sww_frame_wait(agx_pool p, int32_t sid, const float** vertex, const float** centroid);
 
 /* Evolve clock of one scenario (generic_domain.py:1715-1826): relative time,
@@ -144,6 +144,11 @@ agx_status agx_pool_snapshot(agx_pool p);
 agx_status agx_pool_restore(agx_pool p);
 agx_status agx_pool_time_phases(agx_pool p, int32_t reps, double* ms, int32_t n_cat);
 int32_t agx_pool_grid(agx_pool p);
+/* Keep the work records the flux kernels gather resident in L2 through an
+ * access policy window (1) or not (0, the default); timed by the autotuner.
+ * Switching it on sets this context's persisting L2 size to the device's
+ * maximum.  No counterpart in the reference (a GPU cache policy). */
+agx_status agx_pool_set_l2_window(agx_pool p, int32_t on);
 int32_t agx_pool_last_error(char* buf, int32_t n);
 
 #ifdef __cplusplus

@@ -24,9 +24,10 @@ def test_sww_layout_and_host_frame(tmp_path):
     # the mask is taken at the nodes (file/sww.py:380-400): where the node's
     # mean stage minus its mean bed is below minimum_storable_height, the
     # stage stored is the bed and the momenta are zero; centroid values are
-    # stored as they are
-    zn = w._smooth(d.quantities["elevation"].vertex_values)
-    wn = w._smooth(d.quantities["stage"].vertex_values)
+    # stored as they are.  The DE algorithms average centroid values to nodes.
+    assert d.get_using_centroid_averaging()
+    zn = w._smooth(None, d.quantities["elevation"].centroid_values)
+    wn = w._smooth(None, d.quantities["stage"].centroid_values)
     masked = wn - zn < 0.5
     assert masked.any() and (~masked).any()
     assert np.array_equal(f["stage"][0][masked], zn[masked].astype(np.float32))
@@ -38,9 +39,9 @@ def test_sww_layout_and_host_frame(tmp_path):
 
 
 def test_node_means_follow_the_reference_summation_order():
-    """Node means add each node's vertex values one at a time in the order of
-    the mesh's vertex_value_indices and divide by the count
-    (quantity.c:823-870)."""
+    """Node means add each node's vertex values (or the centroid values of
+    its triangles) one at a time in the order of the mesh's
+    vertex_value_indices and divide by the count (quantity.c:823-915)."""
     d = workloads.dam_break(m=5)
     w = SWW_file(d)
     rng = np.random.default_rng(3)
@@ -58,3 +59,13 @@ def test_node_means_follow_the_reference_summation_order():
             q += 1
         want[p] = total / counts[p]
     assert np.array_equal(got, want)
+    cv = rng.normal(size=len(d)) * 1e3
+    got_c = w._smooth(None, cv)
+    q = 0
+    for p in range(d.mesh.number_of_nodes):
+        total = 0.0
+        for _ in range(counts[p]):
+            total += cv[vvi[q] // 3]
+            q += 1
+        want[p] = total / counts[p]
+    assert np.array_equal(got_c, want)
