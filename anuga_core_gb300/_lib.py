@@ -129,6 +129,7 @@ def load(path=None):
         "agx_version": ([], ctypes.c_int32),
         "agx_kernel_launches": ([], ctypes.c_int64),
         "agx_fp64_throughput": ([_f64p, _f64p, _f64p], ctypes.c_int32),
+        "agx_soft64_throughput": ([_f64p], ctypes.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -393,3 +394,13 @@ def fp64_throughput():
 
 def footprint(n_cells, n_boundary, n_edges, precision=AGX_PREC_FP64):
     return int(load().agx_scenario_footprint(n_cells, n_boundary, n_edges, precision))
+
+
+def soft64_throughput():
+    """G op/s of binary64 add, mul, div, sqrt on the FP64 pipe and on the
+    integer pipes (exactly rounded), and half on each for div and mul."""
+    v = np.zeros(10)
+    check(load().agx_soft64_throughput(ptr_f64(v)))
+    keys = ("fp64_add", "fp64_mul", "fp64_div", "fp64_sqrt", "int_add", "int_mul", "int_div", "int_sqrt",
+            "half_div", "half_mul")
+    return dict(zip(keys, v.tolist()))

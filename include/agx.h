@@ -285,6 +285,12 @@ int64_t agx_kernel_launches(void);
  * device: the compute ceiling of the plain FP64 path.  No counterpart in the
  * reference (measurement only); allocates and frees a small result buffer. */
 agx_status agx_fp64_throughput(double* dfma_gops, double* ddiv_gops, double* dsqrt_gops);
+/* Throughput (G op/s) of binary64 add, multiply, divide and square root on
+ * the FP64 pipe (out[0..3]), done with integer instructions with exact IEEE
+ * rounding (out[4..7]; anuga_core_gb300/csrc/soft64.cuh) and split half and
+ * half between the two (divide out[8], multiply out[9]).  No counterpart in
+ * the reference (a GPU measurement). */
+agx_status agx_soft64_throughput(double* out10);
 
 #ifdef __cplusplus
 }

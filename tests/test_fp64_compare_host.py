@@ -9,7 +9,11 @@ host from the same source (de_plain.cuh compiled by g++):
   formulas bit for bit on 4M and 2M random and adversarial inputs;
 * tests/cpp/check_bits.cpp: the mixed update's integer-pipe conversions
   (bits.cuh: f2d_bits, d2f_bits) and RK2 halving (half_sum) equal the
-  operations they replace."""
+  operations they replace;
+* tests/cpp/check_soft64.cpp: the integer-only binary64 add, sub, mul, div
+  and sqrt (soft64.cuh) equal the processor's IEEE operations bit for bit
+  on special values, significands at the ends of their range and 1M random
+  cases of each class."""
 import os
 import shutil
 import subprocess
@@ -42,3 +46,8 @@ def test_limiter_and_wet_dry_factor_match_reference_formulas(tmp_path):
 
 def test_mixed_update_bit_conversions(tmp_path):
     assert "mismatches 0" in _run(tmp_path, "check_bits")
+
+
+def test_integer_binary64_arithmetic_matches_ieee(tmp_path):
+    out = _run(tmp_path, "check_soft64")
+    assert "mismatches 0" in out.splitlines()[-1], out
