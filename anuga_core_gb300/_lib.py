@@ -130,6 +130,8 @@ def load(path=None):
         "agx_kernel_launches": ([], ctypes.c_int64),
         "agx_fp64_throughput": ([_f64p, _f64p, _f64p], ctypes.c_int32),
         "agx_soft64_throughput": ([_f64p], ctypes.c_int32),
+        "agx_soft64_check": ([ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)],
+                             ctypes.c_int32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -404,3 +406,11 @@ def soft64_throughput():
     keys = ("fp64_add", "fp64_mul", "fp64_div", "fp64_sqrt", "int_add", "int_mul", "int_div", "int_sqrt",
             "half_div", "half_mul")
     return dict(zip(keys, v.tolist()))
+
+
+def soft64_check(n, seed=1):
+    """Mismatches of the device's integer-instruction add, sub, mul, div and
+    sqrt against its FP64 pipe over n drawn cases each."""
+    m = (ctypes.c_ulonglong * 5)()
+    check(load().agx_soft64_check(int(n), int(seed), m))
+    return dict(zip(("add", "sub", "mul", "div", "sqrt"), [int(x) for x in m]))

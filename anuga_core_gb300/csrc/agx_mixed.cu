@@ -708,9 +708,9 @@ __device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
           d.vhB[k] = vh;
           d.W2[k] = record_of(P, h, uh, vh);     // work record of the third stage
         } else {                                  // RK3: Q = (2 Q + Q0) / 3
-          h = (2.0 * h + d.wA[k]) / 3.0;
-          uh = (2.0 * uh + d.uhA[k]) / 3.0;
-          vh = (2.0 * vh + d.vhA[k]) / 3.0;
+          h = ddiv(2.0 * h + d.wA[k], 3.0);       // correctly rounded, off the FP64 pipe
+          uh = ddiv(2.0 * uh + d.uhA[k], 3.0);
+          vh = ddiv(2.0 * vh + d.vhA[k], 3.0);
           d.wA[k] = h;
           d.uhA[k] = uh;
           d.vhA[k] = vh;

@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(NA_TPB) k_na_accum(NaArgs a, double* scr, int 
       if (substep == 0) {
         a.b.max_speed[k] = F.smax;
         if (F.smax > 0.0) {
-          const double dt = a.b.radii[k] * 1.0 / F.smax;
+          const double dt = agx::ddiv(a.b.radii[k] * 1.0, F.smax);
           key = ~(unsigned long long)__double_as_longlong(dt);
         }
       }

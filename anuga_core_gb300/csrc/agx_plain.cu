@@ -223,7 +223,7 @@ __global__ void k_accum(Dev d, int substep) {
     if (substep == 0) {
       d.max_speed[k] = F.smax;
       if (F.smax > 0.0) {
-        const double dt = d.radii[k] * 1.0 / F.smax;
+        const double dt = ddiv(d.radii[k] * 1.0, F.smax);
         key = ~(unsigned long long)__double_as_longlong(dt);
       }
     }
@@ -278,9 +278,9 @@ __global__ void k_update(Dev d, int stage, int use_clock_dt, double dt_arg, int 
       uh = a * uh + b * d.uh0[k];
       vh = a * vh + b * d.vh0[k];
       if (saxpy == 3) {
-        w = w / 3.0;
-        uh = uh / 3.0;
-        vh = vh / 3.0;
+        w = ddiv(w, 3.0);
+        uh = ddiv(uh, 3.0);
+        vh = ddiv(vh, 3.0);
       }
     }
     d.w[k] = w;
@@ -331,9 +331,9 @@ __global__ void k_backup(Dev d) {
 __global__ void k_divide(Dev d, double divisor) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.N) return;
-  d.w[k] = d.w[k] / divisor;
-  d.uh[k] = d.uh[k] / divisor;
-  d.vh[k] = d.vh[k] / divisor;
+  d.w[k] = ddiv(d.w[k], divisor);
+  d.uh[k] = ddiv(d.uh[k], divisor);
+  d.vh[k] = ddiv(d.vh[k], divisor);
 }
 
 __global__ void k_saxpy(Dev d, double a, double b) {

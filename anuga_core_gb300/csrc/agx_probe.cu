@@ -43,6 +43,61 @@ __global__ void k_fp64_probe(double* out, int iters, double seed) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;    // keeps the chains live
 }
 
+// ---- device self-check of soft64.cuh against the FP64 pipe ----------------
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {     // splitmix64 finaliser
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ bool same_result(double ref, double got) {
+  const uint64_t r = soft64::bits(ref), g = soft64::bits(got);
+  const bool rn = (r & ~soft64::SIGN) > soft64::EXP_MASK, gn = (g & ~soft64::SIGN) > soft64::EXP_MASK;
+  return rn ? gn : r == g;                    // a NaN only has to be a NaN
+}
+
+// Case i draws a pair (a, b) of one of four classes: any bit pattern; b with
+// an exponent within 35 of a's (cancellation and carries in add/sub); a and
+// b moderate integers times powers of two (exact and tie quotients and
+// products); results near and below the normal range.  mism[0..4] count the
+// add, sub, mul, div and sqrt results that differ from the FP64 pipe's.
+__global__ void k_soft64_check(long long n, uint64_t seed, unsigned long long* mism) {
+  unsigned long long m[5] = {0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t h0 = mix64(seed ^ (uint64_t)i), h1 = mix64(h0), h2 = mix64(h1), h3 = mix64(h2);
+    uint64_t ab = h0, bb = h1;
+    switch (h2 & 3) {
+      case 0:
+        break;
+      case 1: {
+        const int de = (int)(h3 % 71) - 35;
+        bb = (h1 & 0x800fffffffffffffull) | ((((ab >> 52) & 0x7ff) + de) & 0x7ff) << 52;
+        break;
+      }
+      case 2: {
+        const double a = (double)(int64_t)(h0 >> (h3 & 63)) * ldexp(1.0, (int)(h2 >> 8 & 127) - 64);
+        const double b = (double)(int64_t)((h1 >> (h3 >> 6 & 63)) | 1) * ldexp(1.0, (int)(h2 >> 16 & 127) - 64);
+        ab = soft64::bits(a);
+        bb = soft64::bits(b);
+        break;
+      }
+      default:
+        ab = (h0 & 0x800fffffffffffffull) | (uint64_t)(h3 % 64) << 52;           // tiny exponents
+        bb = (h1 & 0x800fffffffffffffull) | (uint64_t)(1023 - (h3 >> 8) % 64) << 52;
+        break;
+    }
+    const double a = soft64::from_bits(ab), b = soft64::from_bits(bb);
+    m[0] += !same_result(__dadd_rn(a, b), soft64::add(a, b));
+    m[1] += !same_result(__dsub_rn(a, b), soft64::sub(a, b));
+    m[2] += !same_result(__dmul_rn(a, b), soft64::mul(a, b));
+    m[3] += !same_result(__ddiv_rn(a, b), soft64::div(a, b));
+    m[4] += !same_result(__dsqrt_rn(a), soft64::sqrt(a));
+  }
+  for (int j = 0; j < 5; j++)
+    if (m[j]) atomicAdd(mism + j, m[j]);
+}
+
 template <int OP>
 cudaError_t time_probe(double* out, int blocks, int iters, double* gops) {
   cudaEvent_t e0, e1;
@@ -105,5 +160,25 @@ extern "C" agx_status agx_soft64_throughput(double* out8) {
   if (e == cudaSuccess) e = time_probe<9>(out, blocks, 64, out8 + 8);
   if (e == cudaSuccess) e = time_probe<10>(out, blocks, 256, out8 + 9);
   cudaFree(out);
+  return e == cudaSuccess ? AGX_OK : AGX_E_CUDA;
+}
+
+// Runs n cases of each soft64.cuh operation on the device against the FP64
+// pipe's IEEE operations; writes the mismatch count of add, sub, mul, div and
+// sqrt to mism5.
+extern "C" agx_status agx_soft64_check(long long n, unsigned long long seed, unsigned long long* mism5) {
+  if (!mism5 || n < 0) return AGX_E_INVALID;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 5 * sizeof(unsigned long long)) != cudaSuccess) return AGX_E_NOMEM;
+  cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+  int dev = 0, sms = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    k_soft64_check<<<4 * sms, 256>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(mism5, d, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
   return e == cudaSuccess ? AGX_OK : AGX_E_CUDA;
 }

@@ -40,6 +40,7 @@
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
+#include "soft64.cuh"
 
 #ifdef __CUDACC__
 #define AGX_HD __host__ __device__ __forceinline__
@@ -78,6 +79,33 @@ AGX_HD bool dle0(double x) { return dkey(x) <= 0; }             // x <= 0
 AGX_HD bool dnz(double x) { return ((uint64_t)dbits(x) << 1) != 0; }   // x != 0
 AGX_HD double dmax(double a, double b) { return dkey(a) >= dkey(b) ? a : b; }
 AGX_HD double dmin(double a, double b) { return dkey(a) <= dkey(b) ? a : b; }
+
+// ---- FP64 division and square root ----------------------------------------
+// Correctly rounded either way, so the results are the same bits.
+// AGX_INT_DIVSQRT selects, for device code, which of the two are formed with
+// integer instructions (soft64.cuh) instead of on the FP64 pipe, which bounds
+// the FP64 kernels: bit 0 division, bit 1 square root.  Measured on GB300 (152
+// SMs): 115 G divisions/s and 93 G square roots/s on the integer pipes against
+// 70 G/s each on the FP64 pipe, and a plain DE1 step of 4.0M triangles
+// 8.37 -> 6.63 ms with both (6.79 with division alone, 8.19 with the square
+// root alone).
+#ifndef AGX_INT_DIVSQRT
+#define AGX_INT_DIVSQRT 3
+#endif
+AGX_HD double ddiv(double a, double b) {
+#if defined(__CUDA_ARCH__) && (AGX_INT_DIVSQRT & 1)
+  return soft64::div(a, b);
+#else
+  return a / b;
+#endif
+}
+AGX_HD double dsqrt(double x) {
+#if defined(__CUDA_ARCH__) && (AGX_INT_DIVSQRT & 2)
+  return soft64::sqrt(x);
+#else
+  return sqrt(x);
+#endif
+}
 
 // ---- boundary kinds ------------------------------------------------------
 enum BoundaryKind : int {
@@ -169,7 +197,7 @@ AGX_HD double prep_cell(const Params& P, int k, double* w, double* uh, double* v
     uk = 0.0;
     vk = 0.0;
   } else if (P.velocity_extrapolation) {
-    const double inv = 1.0 / dk;
+    const double inv = ddiv(1.0, dk);
     ru = uk * inv;
     rv = vk * inv;
   } else {
@@ -202,9 +230,9 @@ AGX_HD double min_failing_ratio(const bool fail[3], const bool neg[3], double lo
   const double db = (fail[0] && fail[1]) ? jump[1] : jump[2];
   const bool three = fail[0] && fail[1] && fail[2];
   if (!(fail[0] || fail[1] || fail[2])) return floor;
-  double r = dmin(na / da, floor);
-  if (two) r = dmin(nb / db, r);
-  if (three) r = dmin(n2 / jump[2], r);
+  double r = dmin(ddiv(na, da), floor);
+  if (two) r = dmin(ddiv(nb, db), r);
+  if (three) r = dmin(ddiv(n2, jump[2]), r);
   return r;
 }
 
@@ -323,10 +351,10 @@ AGX_HD double wet_dry_factor(const Params& P, double hc, double hlo, double hhi)
   if (a1 && b1 && c1) return 1.0;
   // f = max(0, min(A, min(B, 1))), then min(C, f): a term proved >= 1 does
   // not change either minimum, so it is not divided out
-  const double bt = b1 ? 1.0 : dmin(P.c_tmp * dmax(hc, 0.0) / hhi_e + P.d_tmp, 1.0);
-  const double at = a1 ? bt : dmin(P.c_tmp * dmax(hlo, 0.0) / hc_e + P.d_tmp, bt);
+  const double bt = b1 ? 1.0 : dmin(ddiv(P.c_tmp * dmax(hc, 0.0), hhi_e) + P.d_tmp, 1.0);
+  const double at = a1 ? bt : dmin(ddiv(P.c_tmp * dmax(hlo, 0.0), hc_e) + P.d_tmp, bt);
   double f = dmax(0.0, at);
-  if (!c1) f = dmin(1.2 * dmax(hlo - P.hmin, 0.0) / (dmax(hlo, 0.0) + 1.0 * P.hmin), f);
+  if (!c1) f = dmin(ddiv(1.2 * dmax(hlo - P.hmin, 0.0), dmax(hlo, 0.0) + 1.0 * P.hmin), f);
   return f;
 }
 
@@ -456,7 +484,7 @@ AGX_HD void central_flux(const double ql[3], const double qr[3], double hl, doub
   double vhr = -n2 * qr[1] + n1 * qr[2];
   double ul, vl, ur, vr;
   if (dgt0(hle)) {
-    const double inv = 1.0 / hle;
+    const double inv = ddiv(1.0, hle);
     ul = uhl * inv;
     uhl = hl * ul;
     vl = vhl * inv;
@@ -465,7 +493,7 @@ AGX_HD void central_flux(const double ql[3], const double qr[3], double hl, doub
     ul = uhl = vhl = vl = 0.0;
   }
   if (dgt0(hre)) {
-    const double inv = 1.0 / hre;
+    const double inv = ddiv(1.0, hre);
     ur = uhr * inv;
     uhr = hr * ur;
     vr = vhr * inv;
@@ -473,14 +501,14 @@ AGX_HD void central_flux(const double ql[3], const double qr[3], double hl, doub
   } else {
     ur = uhr = vhr = vr = 0.0;
   }
-  const double cl = sqrt(g * hl);
-  const double cr = sqrt(g * hr);
+  const double cl = dsqrt(g * hl);
+  const double cr = dsqrt(g * hr);
   double fs = 1.0;
   if (low_froude == 1) {
-    fs = sqrt(fmax(0.001, fmin(1.0, (ur * ur + ul * ul + vr * vr + vl * vl) / (cl * cl + cr * cr + 1.0e-10))));
+    fs = dsqrt(fmax(0.001, fmin(1.0, ddiv(ur * ur + ul * ul + vr * vr + vl * vl, cl * cl + cr * cr + 1.0e-10))));
   } else if (low_froude == 2) {
-    fs = sqrt((ur * ur + ul * ul + vr * vr + vl * vl) / (cl * cl + cr * cr + 1.0e-10));
-    fs = sqrt(fmin(1.0, 0.01 + fmax(fs - 0.01, 0.0)));
+    fs = dsqrt(ddiv(ur * ur + ul * ul + vr * vr + vl * vl, cl * cl + cr * cr + 1.0e-10));
+    fs = dsqrt(fmin(1.0, 0.01 + fmax(fs - 0.01, 0.0)));
   }
   double smax = dmax(ul + cl, ur + cr);
   if (dkey(smax) < -1) smax = 0.0;          // smax < 0
@@ -494,7 +522,7 @@ AGX_HD void central_flux(const double ql[3], const double qr[3], double hl, doub
     return;
   }
   F.speed = dmax(smax, -smin);
-  const double inv_span = 1.0 / dmax(span, 1.0e-100);
+  const double inv_span = ddiv(1.0, dmax(span, 1.0e-100));
   const double fl0 = ul * hl, fl1 = ul * uhl, fl2 = ul * vhl;
   const double fr0 = ur * hr, fr1 = ur * uhr, fr2 = ur * vhr;
   double f0 = smax * fl0 - smin * fr0;
@@ -744,13 +772,13 @@ AGX_HD void boundary_value(int kind, double n1, double n2, double we, double uhe
 AGX_HD double h_pow_7_3(double h) { return (h * h) * cbrt(h); }
 
 AGX_HD double manning_S(const Params& P, double w, double z, double uh, double vh, double eta) {
-  const double mom = sqrt((uh * uh + vh * vh));
+  const double mom = dsqrt((uh * uh + vh * vh));
   double S = 0.0;
   if (dgt(eta, P.hmin)) {
     const double h = w - z;
     if (dge(h, P.hmin)) {
       S = -P.g * eta * eta * mom;
-      S /= h_pow_7_3(h);
+      S = ddiv(S, h_pow_7_3(h));
     }
   }
   return S;
@@ -764,15 +792,15 @@ AGX_HD double manning_S_sloped(const Params& P, double w, const double* zv3, con
   if (eta > P.hmin) {
     const double det = (y2 - y0) * (x1 - x0) - (y1 - y0) * (x2 - x0);
     double zx = (y2 - y0) * (z1 - z0) - (y1 - y0) * (z2 - z0);
-    zx /= det;
+    zx = ddiv(zx, det);
     double zy = (x1 - x0) * (z2 - z0) - (x2 - x0) * (z1 - z0);
-    zy /= det;
-    const double zs = sqrt(1.0 + zx * zx + zy * zy);
+    zy = ddiv(zy, det);
+    const double zs = dsqrt(1.0 + zx * zx + zy * zy);
     const double zbar = (z0 + z1 + z2) * (1.0 / 3.0);
     const double h = w - zbar;
     if (h >= P.hmin) {
-      S = -P.g * eta * eta * zs * sqrt((uh * uh + vh * vh));
-      S /= h_pow_7_3(h);
+      S = -P.g * eta * eta * zs * dsqrt((uh * uh + vh * vh));
+      S = ddiv(S, h_pow_7_3(h));
     }
   }
   return S;
@@ -783,12 +811,12 @@ AGX_HD bool update_quantity(double& q, double expl, double& semi, double dt) {
   const double x = q;
   double s = semi;
   if (!dnz(x)) s = 0.0;
-  else if (dnz(s)) s /= x;         // 0/x is a zero: the denominator below is then exactly 1
+  else if (dnz(s)) s = ddiv(s, x);         // 0/x is a zero: the denominator below is then exactly 1
   q = q + dt * expl;
   const double den = 1.0 - dt * s;
   semi = 0.0;
   if (dle0(den)) return false;
-  if (dbits(den) != dbits(1.0)) q /= den;
+  if (dbits(den) != dbits(1.0)) q = ddiv(q, den);
   return true;
 }
 

@@ -194,9 +194,26 @@ SF_HD uint64_t mul_bits(uint64_t a, uint64_t b) {
 // Newton-Raphson steps r <- r + r (1 - d r / 2^127) in fixed point.  The
 // result is within a few units of its last place; the quotient built from it
 // is corrected exactly by its remainder.
+// FP32 seeds, rounded to nearest whatever the build's FP32 division and
+// square root flags (fast approximations, flush to zero) say
+SF_HD float recip_rn(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+SF_HD float sqrt_rn(float x) {
+#ifdef __CUDA_ARCH__
+  return __fsqrt_rn(x);
+#else
+  return sqrtf(x);
+#endif
+}
+
 SF_HD uint64_t recip64(uint64_t d) {
   const float x = (float)(d >> 40) * (1.0f / 8388608.0f);            // d / 2^63 in [1, 2)
-  uint64_t r = (uint64_t)((1.0f / x) * 2147483520.0f) << 33;         // ~ 2^64 / x, below 2^64
+  uint64_t r = (uint64_t)(recip_rn(x) * 2147483520.0f) << 33;        // ~ 2^64 / x, below 2^64
   for (int it = 0; it < 2; it++) {
     const uint64_t t = mulhi64(d, r);            // ~ d r / 2^64 ~ 2^63
     if (t <= (1ull << 63)) r += mulhi64(r, ((1ull << 63) - t) << 1);
@@ -258,7 +275,7 @@ SF_HD uint64_t div_bits(uint64_t a, uint64_t b) {
 // Newton-Raphson steps y <- y + y (1 - x y^2) / 2 in fixed point.
 SF_HD uint64_t rsqrt64(uint64_t s) {
   const float x = (float)(s >> 40) * (1.0f / 16777216.0f);          // s / 2^64 in [1/4, 1)
-  uint64_t y = (uint64_t)((1.0f / sqrtf(x)) * 1073741824.0f) << 32; // ~ 2^62 / sqrt(x), at most 2^63
+  uint64_t y = (uint64_t)(recip_rn(sqrt_rn(x)) * 1073741824.0f) << 32;   // ~ 2^62 / sqrt(x), at most 2^63
   for (int it = 0; it < 2; it++) {
     const uint64_t t = mulhi64(s, mulhi64(y, y));    // ~ x y^2 * 2^60
     if (t <= (1ull << 60)) y += mulhi64(y, ((1ull << 60) - t) << 3);

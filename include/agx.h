@@ -291,6 +291,11 @@ agx_status agx_fp64_throughput(double* dfma_gops, double* ddiv_gops, double* dsq
  * half between the two (divide out[8], multiply out[9]).  No counterpart in
  * the reference (a GPU measurement). */
 agx_status agx_soft64_throughput(double* out10);
+/* n cases of each integer-instruction binary64 operation (add, sub, mul,
+ * div, sqrt) run on the device against the FP64 pipe's IEEE results; writes
+ * the number of mismatches of each to mism5 (a NaN result only has to be a
+ * NaN).  No counterpart in the reference (a self-check of this library). */
+agx_status agx_soft64_check(long long n, unsigned long long seed, unsigned long long* mism5);
 
 #ifdef __cplusplus
 }

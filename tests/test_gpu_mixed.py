@@ -244,10 +244,10 @@ def test_snapshot_restore_and_autotune_leave_state_unchanged():
     ref = d1.quantities["stage"].centroid_values.copy()
     d2 = make_domain(p, e, b, "DE1", st, kinds, precision="mixed")
     d2._ensure_device()
-    from anuga_core_gb300.autotune import tune_pool, VARIANTS
+    from anuga_core_gb300.autotune import tune_pool, VARIANTS, NAMES
     pool = d2._scn.pool
     res, best = tune_pool(pool, steps=3, reps=1)
-    assert set(res) == {"r80-persistent", "r80-per-tile", "r64-persistent", "r64-per-tile"}
+    assert set(NAMES.values()) <= set(res) and best in res      # every form timed, the fastest kept
     d2.advance_steps(10)
     got = d2.quantities["stage"].centroid_values
     assert np.array_equal(got, ref)
