@@ -111,6 +111,9 @@ static size_t layout(Scenario* s, char* base) {
   for (double** p : edg) *p = (double*)take(N * 3 * 8);
   double** bnd[] = {&d.wb, &d.uhb, &d.vhb};
   for (double** p : bnd) *p = (double*)take(B * 8);
+  d.order = (int*)take(N * 4);
+  d.cls = (unsigned char*)take(N);
+  d.cls_count = (unsigned int*)take(512 * 4);
   d.clock = (Clock*)take(sizeof(Clock));
   return off;
 }
@@ -304,6 +307,7 @@ agx_status agx_scenario_create(const agx_mesh_desc* m, const agx_params* p, agx_
   s->stream = s->own_stream;
   if (cudaMallocHost(&s->clock_host, sizeof(Clock)) != cudaSuccess) return fin(fail(AGX_E_NOMEM, "pinned clock alloc failed"));
   if (cudaMemsetAsync(arena, 0, bytes, s->stream) != cudaSuccess) return fin(fail(AGX_E_CUDA, "memset failed"));
+  if (enqueue_order_init(s, s->stream) != cudaSuccess) return fin(fail(AGX_E_CUDA, "order init failed"));
   const size_t N = s->N, B = s->B, E = s->E;
   struct Up { const void* src; const void* dst; size_t bytes; } ups[] = {
       {m->conn, s->d.conn, N * 16}, {m->surr, s->d.surr, N * 16}, {m->geo, s->d.geo, N * GEO_STRIDE * 8},

@@ -182,6 +182,12 @@ struct Dev {
   double *sw, *suh, *svh;
   double *max_speed;
   double *sl0, *sl1, *sl2, *slsp, *slpf, *slhl;
+  // the extrapolation's cell order: cells grouped by the branches they took
+  // in the previous extrapolation (cls), so that the lanes of a warp follow
+  // the same path; cls_count[0..255] counts, [256..511] scatter cursors
+  int* order;
+  unsigned char* cls;
+  unsigned int* cls_count;
   Clock* clock;
   // riverwalls (structures/riverwall.py): per slot the 1-based riverwall
   // edge (0: ordinary edge), crest elevation and hydraulic-table row per
@@ -262,5 +268,6 @@ cudaError_t enqueue_backup(Scenario* s, cudaStream_t st);
 cudaError_t enqueue_saxpy(Scenario* s, cudaStream_t st, double a, double b);
 cudaError_t enqueue_divide(Scenario* s, cudaStream_t st, double divisor);
 cudaError_t enqueue_reset_accum(Scenario* s, cudaStream_t st);
+cudaError_t enqueue_order_init(Scenario* s, cudaStream_t st);
 
 }  // namespace agx

@@ -303,11 +303,12 @@ AGX_HD void limited_edges(double qc, const double jump[3], double phi, double ou
   }
 }
 
-AGX_HD void reconstruct3(double beta, double inv_known, double qc, double q0, double q1, double q2,
-                         const double* G, double out[3]) {
+// Returns the limiter's phi (1 where the reconstruction is not limited).
+AGX_HD double reconstruct3(double beta, double inv_known, double qc, double q0, double q1, double q2,
+                           const double* G, double out[3]) {
   if (!dgt0(beta)) {
     out[0] = qc; out[1] = qc; out[2] = qc;
-    return;
+    return 1.0;
   }
   const double d0 = q0 - qc;
   const double d1 = q1 - q0;
@@ -322,6 +323,7 @@ AGX_HD void reconstruct3(double beta, double inv_known, double qc, double q0, do
   const double lo = dmin(dmin(d0, dmin(d0 + d1, d0 + d2)), 0.0);
   const double phi = limiter_phi(jump, lo, hi, beta, inv_known);
   limited_edges(qc, jump, phi, out);
+  return phi;
 }
 
 AGX_HD void reconstruct_towards(double beta, double inv_known, double qc, double qn, const double* G,
@@ -383,10 +385,14 @@ AGX_HD void neighbour_uv(const Params& P, int s, bool before, const int4* surr, 
 }
 
 // Main extrapolation loop body (:1418-1896) for cell k.  Returns true if the
-// cell's centroid momenta must be zeroed (surrounded by dry cells).
+// cell's centroid momenta must be zeroed (surrounded by dry cells).  *cls
+// (if given) receives the branches the cell took: bits 0-1 the boundary
+// class (0: at most one boundary edge, 1: two, 2: three), bit 2 a dry cell,
+// bit 3 a wet/dry factor below 1, bits 4-7 a limited stage, height,
+// x and y reconstruction.
 AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* surr, const double* geo,
                         const double* w, const double* h, const double* u, const double* v,
-                        EdgeOut& E) {
+                        EdgeOut& E, int* cls = nullptr) {
   const int4 s = surr[k];
   const int meta = conn[k].w;
   const int nb = meta_nb(meta);
@@ -396,6 +402,7 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
                     (dlt(h[s.z], P.hmin) | (s.z == k));
   double uk = u[k], vk = v[k];
   if (sdry) { uk = 0.0; vk = 0.0; }
+  int c = (nb == 3 ? 2 : (nb == 2 ? 1 : 0)) | (dlt(hk, P.hmin) ? 4 : 0);
   if (nb == 3) {
     for (int i = 0; i < 3; i++) {
       E.w[i] = w[k]; E.uh[i] = uk; E.vh[i] = vk; E.h[i] = hk;
@@ -409,8 +416,8 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
     const bool one = dbits(hf) == dbits(1.0);
     const double beta = one ? P.beta_w1 : P.beta_w_dry + (P.beta_w - P.beta_w_dry) * hf;
     const double ib = one ? P.inv_beta_w1 : 0.0;
-    reconstruct3(beta, ib, w[k], w[s.x], w[s.y], w[s.z], G, E.w);
-    reconstruct3(beta, ib, hk, h0, h1, h2, G, E.h);
+    const double pw = reconstruct3(beta, ib, w[k], w[s.x], w[s.y], w[s.z], G, E.w);
+    const double ph = reconstruct3(beta, ib, hk, h0, h1, h2, G, E.h);
     const double beta_u = one ? P.beta_uh1 : P.beta_uh_dry + (P.beta_uh - P.beta_uh_dry) * hf;
     const double beta_v = one ? P.beta_vh1 : P.beta_vh_dry + (P.beta_vh - P.beta_vh_dry) * hf;
     double u0 = u[s.x], u1 = u[s.y], u2 = u[s.z];
@@ -430,8 +437,10 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
       if (s.y == k) { u1 = uk; v1 = vk; }
       if (s.z == k) { u2 = uk; v2 = vk; }
     }
-    reconstruct3(beta_u, one ? P.inv_beta_uh1 : 0.0, uk, u0, u1, u2, G, E.uh);
-    reconstruct3(beta_v, one ? P.inv_beta_vh1 : 0.0, vk, v0, v1, v2, G, E.vh);
+    const double pu = reconstruct3(beta_u, one ? P.inv_beta_uh1 : 0.0, uk, u0, u1, u2, G, E.uh);
+    const double pv = reconstruct3(beta_v, one ? P.inv_beta_vh1 : 0.0, vk, v0, v1, v2, G, E.vh);
+    c |= (one ? 0 : 8) | (dbits(pw) != dbits(1.0) ? 16 : 0) | (dbits(ph) != dbits(1.0) ? 32 : 0) |
+         (dbits(pu) != dbits(1.0) ? 64 : 0) | (dbits(pv) != dbits(1.0) ? 128 : 0);
   } else {
     int j = 0;
     const int sv[3] = {s.x, s.y, s.z};
@@ -452,6 +461,7 @@ AGX_HD bool extrap_cell(const Params& P, int k, const int4* conn, const int4* su
     }
   }
   for (int i = 0; i < 3; i++) E.z[i] = E.w[i] - E.h[i];
+  if (cls) *cls = c;
   return sdry;
 }
 

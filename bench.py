@@ -391,8 +391,9 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
     if precision == "fp64":
         fp = _lib.fp64_throughput()
         roof["fp64_measured"] = fp
-        roof["note"] = ("FP64-pipe bound: the measured FP64 rates (fp64_measured, G ops/s) are 1/54 of the FP32 "
-                        "rate; ncu shows the extrapolation kernel's FP64 pipe 84% busy at 6% of HBM bandwidth")
+        roof["fp64"] = fp64_roofline(N, ms_per_step, fp["dfma_gops"])
+        roof["note"] = ("FP64-pipe bound, not HBM bound: GB300 runs FP64 at 1/54 of its FP32 rate "
+                        "(fp64_measured, G ops/s); roofline.fp64 puts the step against the measured DFMA rate")
     alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
     ach_s = alg_step / (ms_per_step / 1e3) / 1e9
     step_roof = {"achieved": ach_s, "peak": hbm, "unit": "GB/s", "frac": ach_s / hbm,
@@ -432,6 +433,34 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # DRAM traffic per cell-step of the dominant kernel category, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum summed over that
 # category's launches of one step, divided by the cells of the captured mesh).
+# FP64-pipe instructions per cell of one DE1 step (two stages) of the plain
+# path, from one ncu capture (sm__thread_inst_executed_pipe_fp64_pred_on.sum:
+# lanes that did work; sm__inst_executed_pipe_fp64.sum x 32: lane slots the
+# warps occupied, idle lanes of divergent branches included) of each kernel
+# of a stage (prep, extrapolation, flux, accumulation, update) on the
+# 1.0M-triangle inflow_bumps case, divided by its cells, times two stages.
+FP64_PER_CELL_STEP = {
+    "lane_ops": 2 * (7.423 + 102.7 + 102.9 + 69.63 + 53.93),
+    "warp_slots": 2 * 32 * (2.377e5 + 4.140e6 + 3.516e6 + 2.180e6 + 1.737e6) / 1.0e6,
+    "note": "ncu --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,sm__inst_executed_pipe_fp64.sum of "
+            "k_prep, k_extrap<0>, k_flux, k_accum, k_update on the 1.0M-triangle inflow_bumps case (m=500), "
+            "per cell and launch, x 2 stages of a DE1 step"}
+
+
+def fp64_roofline(cells, ms_per_step, dfma_gops):
+    """The plain step against the FP64 pipe: FP64 lane operations per second
+    (the instructions the step issues per cell x cells / step time) over the
+    measured DFMA rate, and the same for the lane slots the warps occupied."""
+    sec = ms_per_step / 1e3
+    ach = FP64_PER_CELL_STEP["lane_ops"] * cells / sec / 1e9
+    occ = FP64_PER_CELL_STEP["warp_slots"] * cells / sec / 1e9
+    return {"bound": "fp64", "achieved": ach, "peak": dfma_gops, "unit": "G FP64 lane-ops/s",
+            "frac": ach / dfma_gops, "slots_achieved": occ, "slots_frac": occ / dfma_gops,
+            "lane_ops_per_cell_step": FP64_PER_CELL_STEP["lane_ops"],
+            "warp_slots_per_cell_step": FP64_PER_CELL_STEP["warp_slots"],
+            "peak_kind": "measured live (agx_fp64_throughput, DFMA)", "note": FP64_PER_CELL_STEP["note"]}
+
+
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
         "bytes_per_cell": (117.617408e6 + 10.710272e6 + 169.683968e6 + 23.024640e6) / 1.0e6,
