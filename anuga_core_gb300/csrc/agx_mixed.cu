@@ -525,7 +525,22 @@ __device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
     float ew = 0.f, ex = 0.f, ey = 0.f, smax = 0.f, bfl = 0.f;
     float4 g3 = make_float4(0.f, 0.f, 0.f, 0.f), g4 = g3;
     double sw = 0.0, suh = 0.0, svh = 0.0;
-    if (valid) {
+    // A cell whose three edges are dry on both sides (edge depths exactly
+    // zero; no boundary, riverwall or unstaged neighbour) has a zero flux:
+    // every term the loop below would add is +0 (both Audusse depths are
+    // zero, so the flux, the speed and the pressure terms vanish), so the
+    // loop and its geometry loads are skipped with the same result.
+    bool dry = valid && cn.x >= 0 && cn.y >= 0 && cn.z >= 0 && !(EXT && ((cn.w >> 20) & 7));
+    if (dry) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const int li = (lk >> (10 * i)) & 1023;
+        const float lh = es[threadIdx.x * 3 + i].h;
+        const float rh = li != LNK_INLINE ? es[li * 3 + nedge_of(cn.w, i)].h : 1.0f;
+        dry = dry && lh == 0.0f && rh == 0.0f;
+      }
+    }
+    if (valid && !dry) {
       const float4 g2 = d.g2[k];
       g3 = d.g3[k];
       g4 = d.g4[k];
