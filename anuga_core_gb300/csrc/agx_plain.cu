@@ -35,13 +35,16 @@ constexpr int TPB = 256;
 // 1: the step's extrapolations visit the cells grouped by the branches each
 // took in the previous extrapolation (per-cell results do not depend on the
 // order in which cells are visited).  Measured on the 4.0M-triangle DE1 step:
-// extrapolation 2.76 -> 2.38 ms, step 6.53 -> 6.21 ms with the sort once per
-// step (6.25 with a sort after every stage).
+// extrapolation 2.76 -> 2.31 ms, step 6.53 -> 6.12 ms with the sort once per
+// step on the dry and wet/dry-factor classes.
 #ifndef AGX_EXTRAP_ORDER
 #define AGX_EXTRAP_ORDER 1
 #endif
 // 1: the cells are sorted after every extrapolation of a step; 2: only after
 // its last (the step's stages visit the cells in one order)
+#ifndef AGX_CLASS_BITS
+#define AGX_CLASS_BITS 2
+#endif
 #ifndef AGX_SORT_CADENCE
 #define AGX_SORT_CADENCE 2
 #endif
@@ -120,7 +123,21 @@ __global__ void __launch_bounds__(TPB, AGX_MINB_EXTRAP) k_extrap(Dev d) {
   EdgeOut E;
   int cls = 0;
   const bool sdry = extrap_cell(d.P, k, d.conn, d.surr, d.geo, d.w, d.h, d.u, d.v, E, ORD ? &cls : nullptr);
-  if (ORD) d.cls[k] = (unsigned char)cls;
+  if (ORD) {
+    // the classes the sort distinguishes: all eight bits, or the four
+    // limiter bits merged into one (5), or none of them (4), or only the
+    // dry and wet/dry-factor bits (2), or only the dry bit (1).  Measured
+    // extrapolation per 4.0M-triangle DE1 step: 2.38, 2.39, 2.31, 2.31,
+    // 2.73 ms (2.76 unsorted): what pays is keeping the cells of the wet/dry
+    // fronts (factor below 1: the divided-out factor, mixed betas, limiter
+    // products) out of the warps of the rest; finer classes only cut the
+    // cells' runs shorter.
+    if (AGX_CLASS_BITS == 5) cls = (cls & 15) | ((cls & 240) ? 16 : 0);
+    if (AGX_CLASS_BITS == 4) cls &= 15;
+    if (AGX_CLASS_BITS == 2) cls &= 12;
+    if (AGX_CLASS_BITS == 1) cls &= 4;
+    d.cls[k] = (unsigned char)cls;
+  }
   const size_t b = 3 * (size_t)k;
 #pragma unroll
   for (int i = 0; i < 3; i++) {

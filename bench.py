@@ -391,7 +391,8 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
     if precision == "fp64":
         fp = _lib.fp64_throughput()
         roof["fp64_measured"] = fp
-        roof["fp64"] = fp64_roofline(N, ms_per_step, fp["dfma_gops"])
+        # the FP64 instruction counts per cell were captured on the inflow_bumps mesh
+        roof["fp64"] = fp64_roofline(N, ms_per_step, fp["dfma_gops"]) if args.workload == "inflow_bumps" else None
         roof["note"] = ("FP64-pipe bound, not HBM bound: GB300 runs FP64 at 1/54 of its FP32 rate "
                         "(fp64_measured, G ops/s); roofline.fp64 puts the step against the measured DFMA rate")
     alg_step = ALG_BYTES_PER_CELL_STEP[precision] * N
@@ -440,10 +441,10 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # of a stage (prep, extrapolation, flux, accumulation, update) on the
 # 1.0M-triangle inflow_bumps case, divided by its cells, times two stages.
 FP64_PER_CELL_STEP = {
-    "lane_ops": 2 * (7.423 + 102.7 + 102.9 + 69.63 + 53.93),
-    "warp_slots": 2 * 32 * (2.377e5 + 4.140e6 + 3.516e6 + 2.180e6 + 1.737e6) / 1.0e6,
+    "lane_ops": 2 * (7.241 + 102.7 + 102.9 + 68.63 + 52.47),
+    "warp_slots": 2 * 32 * (2.318e5 + 3.958e6 + 3.516e6 + 2.148e6 + 1.690e6) / 1.0e6,
     "note": "ncu --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,sm__inst_executed_pipe_fp64.sum of "
-            "k_prep, k_extrap<0>, k_flux, k_accum, k_update on the 1.0M-triangle inflow_bumps case (m=500), "
+            "k_prep, k_extrap<0,1>, k_flux, k_accum, k_update on the 1.0M-triangle inflow_bumps case (m=500), "
             "per cell and launch, x 2 stages of a DE1 step"}
 
 
@@ -463,15 +464,15 @@ def fp64_roofline(cells, ms_per_step, dfma_gops):
 
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
-        "bytes_per_cell": (117.617408e6 + 10.710272e6 + 169.683968e6 + 23.024640e6) / 1.0e6,
+        "bytes_per_cell": (113.140224e6 + 14.782720e6 + 165.193216e6 + 32.142336e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
                 "(m=500, MINB=8 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
                 "scaled by cells"},
     ("fp64", "extrap"): {
-        "bytes_per_cell": 2 * (125.701632e6 + 78.489088e6) / 1.0e6,
-        "note": "ncu --set full of k_extrap<0> (edges only, flowing state) on the 1.0M-triangle inflow_bumps "
-                "case (m=500), dram__bytes_read.sum + dram__bytes_write.sum per launch x 2 launches per "
-                "DE1 step, scaled by cells"},
+        "bytes_per_cell": 2 * (137.848576e6 + 85.762944e6) / 1.0e6,
+        "note": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum of k_extrap<0,1> (edges only, cells in "
+                "branch-class order, flowing state) on the 1.0M-triangle inflow_bumps case (m=500), per launch x 2 "
+                "launches per DE1 step, scaled by cells"},
 }
 
 
