@@ -351,8 +351,24 @@ __global__ void __launch_bounds__(TPB, AGX_MINB_ACCUM) k_accum(Dev d, int subste
       const int n = i == 0 ? c.x : i == 1 ? c.y : c.z;
       fn[i] = n >= 0 ? meta_full(d.conn[n].w) : 1;
     }
+    // A dry cell whose three slots carry a zero flux, no speed, a +0 pressure
+    // flux and zero depths on both sides: every term of accum_cell is then
+    // a zero, its sums and the pressure terms come out +0 (the pressure
+    // bracket is +0 - +0 - (+0 * dz) = +0 whatever the sign of dz), so the
+    // FP64 arithmetic is skipped with the same bits.
+    bool dry = !dnz(d.h[k]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+      dry = dry && !dnz(R[i].f[0]) && !dnz(R[i].f[1]) && !dnz(R[i].f[2]) && dbits(R[i].pflux) == 0 &&
+            !dnz(R[i].hleft) && !dnz(d.he[3 * (size_t)k + i]) && !dgt(R[i].speed, d.P.epsilon);
     CellFlux F;
-    accum_cell(d.P, k, c, R, d.he, d.ze, d.h, d.z, d.normals, d.lengths, d.inv_area[k], fn, F);
+    if (dry) {
+      F.ew = F.euh = F.evh = 0.0 * d.inv_area[k];     // +0 * (1/area), as the sums' scaling
+      F.smax = 0.0;
+      F.bflux = 0.0;
+    } else {
+      accum_cell(d.P, k, c, R, d.he, d.ze, d.h, d.z, d.normals, d.lengths, d.inv_area[k], fn, F);
+    }
     d.xw[k] = F.ew;
     d.xuh[k] = F.euh;
     d.xvh[k] = F.evh;

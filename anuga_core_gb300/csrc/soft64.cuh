@@ -9,8 +9,11 @@
 // SMs: DFMA 525 G op/s, DDIV and DSQRT 70 G op/s), while its integer pipes
 // issue several warp instructions per clock per SM.  An exact binary64
 // operation built from 32- and 64-bit integer arithmetic therefore runs beside
-// the FP64 pipe, and a division or square root of a few dozen integer
-// instructions outruns the pipe's own.  Every non-NaN result is bitwise the
+// the FP64 pipe.  Measured on the same part: division 115 G op/s and square
+// root 93 G op/s this way, faster than the FP64 pipe's; addition (276 G op/s)
+// and multiplication (384 G op/s) slower, and no faster split between the
+// two paths, since both take issue slots.  So the FP64 kernels divide and
+// take square roots with these functions and add and multiply on the pipe.  Every non-NaN result is bitwise the
 // IEEE result; tests/cpp/check_soft64.cpp checks that on the host against the
 // processor's own IEEE arithmetic.
 //
