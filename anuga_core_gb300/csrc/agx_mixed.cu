@@ -484,6 +484,10 @@ __device__ __forceinline__ float step_timestep32(const PoolScn* S, double ts) {
 #ifndef AGX_GEO_PREFETCH
 #define AGX_GEO_PREFETCH 1
 #endif
+// 1: also the geometry blocks the cell's reconstruction reads
+#ifndef AGX_REC_PREFETCH
+#define AGX_REC_PREFETCH 0
+#endif
 __device__ __forceinline__ void prefetch_line(const void* p) {
 #if AGX_STATE_PREFETCH == 1
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -505,6 +509,16 @@ __device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
     const int4 cn_s = d.conn[k];
     const int lk_s = d.lnk[k];
     const float4 rk_s = W[k];
+    const int2 ht = d.tile_halo[tile];
+    const int sid = d.tile_scn[tile];
+    if (sid < 0) continue;
+    PoolScn* S = d.scn + sid;
+    if (!S->active) continue;
+    if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
+    if (STG == 2 && S->P.rk3) continue;       // RK3 scenarios take STG 4 and 3
+    if (STG >= 3 && !S->P.rk3) continue;
+    // prefetches only for the tiles of running scenarios (free tiles and
+    // finished scenarios' tiles skip the work and need no data)
     if (FUSED2 && AGX_STATE_PREFETCH) {        // k lies inside every per-cell array of the pool
       prefetch_line(d.wB + k);
       prefetch_line(d.uhB + k);
@@ -518,14 +532,12 @@ __device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
       }
     }
     if (AGX_GEO_PREFETCH) prefetch_line(d.g3 + k);   // read only by the flux loop
-    const int2 ht = d.tile_halo[tile];
-    const int sid = d.tile_scn[tile];
-    if (sid < 0) continue;
-    PoolScn* S = d.scn + sid;
-    if (!S->active) continue;
-    if (FUSED2 && !S->P.rk2) continue;        // Euler scenarios have one stage
-    if (STG == 2 && S->P.rk3) continue;       // RK3 scenarios take STG 4 and 3
-    if (STG >= 3 && !S->P.rk3) continue;
+    if (AGX_REC_PREFETCH) {                            // read by the reconstruction
+      prefetch_line(d.g0 + k);
+      prefetch_line(d.g1 + k);
+      prefetch_line(d.g2 + k);
+      prefetch_line(d.g4 + k);
+    }
     const MParams P = S->P;
     const double ts_w = FUSED2 ? warp_timestep<LOCALDT>(d, S) : 0.0;     // the step's timestep
     const bool valid = k < S->cell0 + S->ncell;
