@@ -441,8 +441,8 @@ def measure_single(args, precision, torch, world, barrier, dist, builder):
 # of a stage (prep, extrapolation, flux, accumulation, update) on the
 # 1.0M-triangle inflow_bumps case, divided by its cells, times two stages.
 FP64_PER_CELL_STEP = {
-    "lane_ops": 2 * (7.241 + 102.7 + 102.9 + 68.63 + 52.47),
-    "warp_slots": 2 * 32 * (2.318e5 + 3.958e6 + 3.516e6 + 2.148e6 + 1.690e6) / 1.0e6,
+    "lane_ops": 2 * (7.241 + 102.7 + 102.9 + 55.64 + 52.47),
+    "warp_slots": 2 * 32 * (2.318e5 + 3.958e6 + 3.516e6 + 1.820e6 + 1.690e6) / 1.0e6,
     "note": "ncu --metrics sm__thread_inst_executed_pipe_fp64_pred_on.sum,sm__inst_executed_pipe_fp64.sum of "
             "k_prep, k_extrap<0,1>, k_flux, k_accum, k_update on the 1.0M-triangle inflow_bumps case (m=500), "
             "per cell and launch, x 2 stages of a DE1 step"}
@@ -464,7 +464,7 @@ def fp64_roofline(cells, ms_per_step, dfma_gops):
 
 TRAFFIC_PER_STEP = {
     ("mixed", "flux"): {
-        "bytes_per_cell": (113.140224e6 + 14.782720e6 + 165.193216e6 + 32.142336e6) / 1.0e6,
+        "bytes_per_cell": (117.678592e6 + 15.682304e6 + 177.783552e6 + 32.170752e6) / 1.0e6,
         "note": "ncu --set full of k_pool_flux stage 1 + stage 2 on the 1.0M-triangle inflow_bumps case "
                 "(m=500, MINB=8 variant), dram__bytes_read.sum + dram__bytes_write.sum per step, "
                 "scaled by cells"},
