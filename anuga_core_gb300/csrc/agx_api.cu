@@ -335,8 +335,13 @@ agx_status agx_scenario_destroy(agx_handle h) {
   if (s->node_off) cudaFree(s->node_off);
   if (s->node_slot) cudaFree(s->node_slot);
   if (s->frame) cudaFree(s->frame);
+  if (s->copy_stream) {
+    cudaStreamSynchronize(s->copy_stream);
+    cudaStreamDestroy(s->copy_stream);
+  }
   if (s->frame_host) cudaFreeHost(s->frame_host);
   if (s->frame_done) cudaEventDestroy(s->frame_done);
+  if (s->frame_ready) cudaEventDestroy(s->frame_ready);
   if (s->bseries) cudaFree(s->bseries);
   if (s->rw_mem) cudaFree(s->rw_mem);
   if (s->stream) cudaStreamSynchronize(s->stream);
@@ -401,11 +406,13 @@ agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, co
   if (h->node_off) cudaFree(h->node_off);
   if (h->node_slot) cudaFree(h->node_slot);
   if (h->frame) cudaFree(h->frame);
+  if (h->copy_stream) CK(cudaStreamSynchronize(h->copy_stream));
   if (h->frame_host) cudaFreeHost(h->frame_host);
   if (h->frame_done) cudaEventDestroy(h->frame_done);
+  if (h->frame_ready) cudaEventDestroy(h->frame_ready);
   h->node_off = h->node_slot = nullptr;
   h->frame = h->frame_host = nullptr;
-  h->frame_done = nullptr;
+  h->frame_done = h->frame_ready = nullptr;
   h->P = (int)P;
   const size_t fbytes = ((size_t)3 * P + 3 * (size_t)h->N) * 4 + 4;
   CK(cudaMalloc(&h->node_off, (size_t)(P + 1) * 4));
@@ -413,6 +420,8 @@ agx_status agx_sww_bind(agx_handle h, int64_t P, const int32_t* node_offsets, co
   CK(cudaMalloc(&h->frame, fbytes));
   CK(cudaMallocHost(&h->frame_host, fbytes));
   CK(cudaEventCreateWithFlags(&h->frame_done, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&h->frame_ready, cudaEventDisableTiming));
+  if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
   CK(cudaMemcpyAsync(h->node_off, node_offsets, (size_t)(P + 1) * 4, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->node_slot, node_slots, (size_t)3 * h->N * 4, cudaMemcpyHostToDevice, h->stream));
   return sync(h);
@@ -423,6 +432,7 @@ agx_status agx_sww_frame(agx_handle h, double min_storable_height, int32_t centr
   AGX_TRACE("agx_sww_frame");
   if (!h || !vertex_out || !centroid_out) return fail(AGX_E_INVALID, "bad arguments");
   if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
+  CK(cudaStreamWaitEvent(h->stream, h->frame_done, 0));     // an earlier asynchronous copy of the buffer
   CK(enqueue_sww_frame(h, h->stream, min_storable_height, centroid_averaging ? 1 : 0));
   if (h->P > 0) CK(cudaMemcpyAsync(vertex_out, h->frame, (size_t)3 * h->P * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(centroid_out, h->frame + 3 * (size_t)h->P, (size_t)3 * h->N * 4, cudaMemcpyDeviceToHost, h->stream));
@@ -433,10 +443,15 @@ agx_status agx_sww_frame_async(agx_handle h, double min_storable_height, int32_t
   AGX_TRACE("agx_sww_frame_async");
   if (!h) return fail(AGX_E_INVALID, "null handle");
   if (!h->frame) return fail(AGX_E_STATE, "agx_sww_bind first");
+  // the frame kernels wait for the previous frame's copy to leave the buffer;
+  // the copy runs on its own stream, so the steps enqueued next overlap it
+  CK(cudaStreamWaitEvent(h->stream, h->frame_done, 0));
   CK(enqueue_sww_frame(h, h->stream, min_storable_height, centroid_averaging ? 1 : 0));
+  CK(cudaEventRecord(h->frame_ready, h->stream));
+  CK(cudaStreamWaitEvent(h->copy_stream, h->frame_ready, 0));
   CK(cudaMemcpyAsync(h->frame_host, h->frame, ((size_t)3 * h->P + 3 * (size_t)h->N) * 4, cudaMemcpyDeviceToHost,
-                     h->stream));
-  CK(cudaEventRecord(h->frame_done, h->stream));
+                     h->copy_stream));
+  CK(cudaEventRecord(h->frame_done, h->copy_stream));
   return AGX_OK;
 }
 

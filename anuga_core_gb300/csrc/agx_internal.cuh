@@ -209,6 +209,8 @@ struct Scenario {
   float* frame = nullptr;
   float* frame_host = nullptr;           // pinned copy of the last frame (asynchronous output)
   cudaEvent_t frame_done = nullptr;      // recorded after that copy
+  cudaEvent_t frame_ready = nullptr;     // recorded after the frame kernels
+  cudaStream_t copy_stream = nullptr;    // the copy's own stream: the next steps need not wait for it
   agx_params prm{};
   Dev d{};
   void* arena = nullptr;

@@ -1364,6 +1364,8 @@ struct ScnHost {
   float* frame = nullptr;
   float* frame_host = nullptr;
   cudaEvent_t frame_done = nullptr;
+  cudaEvent_t frame_ready = nullptr;      // after the frame kernels
+  cudaStream_t copy_stream = nullptr;     // the frame copy's own stream
   int N = 0, B = 0, tile0 = 0, ntile = 0, bnd0 = 0, halo0 = 0, nhalo = 0;
   agx_params prm{};
   int* order = nullptr;          // device [N]: original index of each stored cell
@@ -1483,14 +1485,20 @@ using namespace agx;
 struct agx_pool_s : public agx::Pool {};
 
 static void free_sww(ScnHost& s) {
+  if (s.copy_stream) {
+    cudaStreamSynchronize(s.copy_stream);
+    cudaStreamDestroy(s.copy_stream);
+  }
   if (s.sww_off) cudaFree(s.sww_off);
   if (s.sww_slot) cudaFree(s.sww_slot);
   if (s.frame) cudaFree(s.frame);
   if (s.frame_host) cudaFreeHost(s.frame_host);
   if (s.frame_done) cudaEventDestroy(s.frame_done);
+  if (s.frame_ready) cudaEventDestroy(s.frame_ready);
   s.sww_off = s.sww_slot = nullptr;
   s.frame = s.frame_host = nullptr;
-  s.frame_done = nullptr;
+  s.frame_done = s.frame_ready = nullptr;
+  s.copy_stream = nullptr;
   s.sww_P = 0;
 }
 
@@ -2661,6 +2669,8 @@ agx_status agx_pool_sww_bind(agx_pool p, int32_t sid, int64_t P, const int32_t* 
   PCK(cudaMalloc(&sh.frame, fbytes));
   PCK(cudaMallocHost(&sh.frame_host, fbytes));
   PCK(cudaEventCreateWithFlags(&sh.frame_done, cudaEventDisableTiming));
+  PCK(cudaEventCreateWithFlags(&sh.frame_ready, cudaEventDisableTiming));
+  PCK(cudaStreamCreateWithFlags(&sh.copy_stream, cudaStreamNonBlocking));
   sh.sww_P = (int)P;
   PCK(cudaMemcpyAsync(sh.sww_off, node_offsets, (size_t)(P + 1) * 4, cudaMemcpyHostToDevice, p->stream));
   PCK(cudaMemcpyAsync(sh.sww_slot, node_slots, (size_t)S3 * 4, cudaMemcpyHostToDevice, p->stream));
@@ -2675,6 +2685,9 @@ agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable
   agx_status st = ensure_work(p, sid);
   if (st) return st;
   cudaStream_t s = p->stream;
+  // the frame kernels wait for the previous frame's copy to leave the buffer;
+  // the copy runs on its own stream, so the steps enqueued next overlap it
+  PCK(cudaStreamWaitEvent(s, sh.frame_done, 0));
   if (sh.sww_P > 0) {
     k_pool_sww_nodes<<<nblk1(sh.sww_P), 256, 0, s>>>(p->d, sid, sh.sww_P, sh.sww_off, sh.sww_slot, sh.inv,
                                                     min_storable_height, centroid_averaging ? 1 : 0, sh.frame);
@@ -2683,9 +2696,11 @@ agx_status agx_pool_sww_frame_async(agx_pool p, int32_t sid, double min_storable
   k_pool_sww_cells<<<nblk1(sh.N), 256, 0, s>>>(p->d, sid, sh.order, sh.frame + 3 * (size_t)sh.sww_P);
   count_launch();
   PCK(cudaGetLastError());
+  PCK(cudaEventRecord(sh.frame_ready, s));
+  PCK(cudaStreamWaitEvent(sh.copy_stream, sh.frame_ready, 0));
   PCK(cudaMemcpyAsync(sh.frame_host, sh.frame, ((size_t)3 * sh.sww_P + 3 * (size_t)sh.N) * 4,
-                      cudaMemcpyDeviceToHost, s));
-  PCK(cudaEventRecord(sh.frame_done, s));
+                      cudaMemcpyDeviceToHost, sh.copy_stream));
+  PCK(cudaEventRecord(sh.frame_done, sh.copy_stream));
   return AGX_OK;
 }
 
