@@ -484,10 +484,6 @@ __device__ __forceinline__ float step_timestep32(const PoolScn* S, double ts) {
 #ifndef AGX_GEO_PREFETCH
 #define AGX_GEO_PREFETCH 1
 #endif
-// 1: also the geometry blocks the cell's reconstruction reads
-#ifndef AGX_REC_PREFETCH
-#define AGX_REC_PREFETCH 0
-#endif
 __device__ __forceinline__ void prefetch_line(const void* p) {
 #if AGX_STATE_PREFETCH == 1
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -532,12 +528,6 @@ __device__ __forceinline__ void flux_phase(const PoolDev& d, EdgeState* es) {
       }
     }
     if (AGX_GEO_PREFETCH) prefetch_line(d.g3 + k);   // read only by the flux loop
-    if (AGX_REC_PREFETCH) {                            // read by the reconstruction
-      prefetch_line(d.g0 + k);
-      prefetch_line(d.g1 + k);
-      prefetch_line(d.g2 + k);
-      prefetch_line(d.g4 + k);
-    }
     const MParams P = S->P;
     const double ts_w = FUSED2 ? warp_timestep<LOCALDT>(d, S) : 0.0;     // the step's timestep
     const bool valid = k < S->cell0 + S->ncell;
