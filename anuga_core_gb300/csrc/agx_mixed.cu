@@ -31,6 +31,7 @@
 #include <cstring>
 #include <cstdio>
 #include <map>
+#include "free_runs.h"
 
 namespace agx {
 
@@ -1371,6 +1372,7 @@ struct Pool {
   int device = 0;
   int cap_cells = 0, cap_tiles = 0, cap_bnd = 0, cap_scn = 0, cap_halo = 0;
   std::vector<int> halo_owner;   // host: halo slot owner (-1 free)
+  FreeRuns free_tiles, free_bnd, free_halo;
   PoolDev d{};
   void* arena = nullptr;
   size_t arena_bytes = 0;
@@ -1791,6 +1793,9 @@ agx_status agx_pool_create(int64_t cap_cells, int64_t cap_boundary, int32_t cap_
   p->tile_scn.assign(p->cap_tiles, -1);
   p->bnd_owner.assign(p->cap_bnd, -1);
   p->halo_owner.assign(p->cap_halo, -1);
+  p->free_tiles.init(p->cap_tiles);
+  p->free_bnd.init(p->cap_bnd);
+  p->free_halo.init(p->cap_halo);
   p->scn.resize(p->cap_scn);
   PCK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
   p->stream = p->own_stream;
@@ -1892,28 +1897,16 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
     p->graph_valid = false;
   }
   const int nt = (int)((N + TILE - 1) / TILE);
-  int t0 = -1;
-  for (int t = 0, run = 0; t < p->cap_tiles; t++) {
-    run = p->tile_scn[t] < 0 ? run + 1 : 0;
-    if (run == nt) { t0 = t - nt + 1; break; }
-  }
+  const int t0 = (int)p->free_tiles.find(nt);            // first fit: the lowest free run
   if (t0 < 0) return pfail(AGX_E_NOMEM, "pool has no %d free contiguous tiles", nt);
   int b0 = 0;
   if (B > 0) {
-    b0 = -1;
-    for (int b = 0, run = 0; b < p->cap_bnd; b++) {
-      run = p->bnd_owner[b] < 0 ? run + 1 : 0;
-      if (run == B) { b0 = b - (int)B + 1; break; }
-    }
+    b0 = (int)p->free_bnd.find(B);
     if (b0 < 0) return pfail(AGX_E_NOMEM, "pool has no %lld free boundary slots", (long long)B);
   }
   int h0 = 0;
   if (n_halo > 0) {
-    h0 = -1;
-    for (int h = 0, run = 0; h < p->cap_halo; h++) {
-      run = p->halo_owner[h] < 0 ? run + 1 : 0;
-      if (run == n_halo) { h0 = h - (int)n_halo + 1; break; }
-    }
+    h0 = (int)p->free_halo.find(n_halo);
     if (h0 < 0) return pfail(AGX_E_NOMEM, "pool has no %lld free halo slots", (long long)n_halo);
   }
   for (int t = 0; t < nt; t++) {
@@ -2003,9 +1996,11 @@ agx_status agx_pool_add(agx_pool p, int64_t N, int64_t B, const int32_t* conn, c
   for (int t = t0; t < t0 + nt; t++) p->tile_scn[t] = sid;
   for (int b = b0; b < b0 + B; b++) p->bnd_owner[b] = sid;
   for (int h = h0; h < h0 + n_halo; h++) p->halo_owner[h] = sid;
-  int ntiles = 0;
-  for (int t = 0; t < p->cap_tiles; t++) if (p->tile_scn[t] >= 0) ntiles = t + 1;
-  PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, st));
+  p->free_tiles.take(t0, nt);
+  if (B > 0) p->free_bnd.take(b0, B);
+  if (n_halo > 0) p->free_halo.take(h0, n_halo);
+  const int ntiles = (int)p->free_tiles.used_end();
+  PCK(cudaMemcpyAsync(p->tile_scn_dev + t0, p->tile_scn.data() + t0, (size_t)nt * 4, cudaMemcpyHostToDevice, st));
   agx_status s2 = pull_scn(p);
   if (s2) return s2;
   PoolScn& S = p->scn_host[sid];
@@ -2047,7 +2042,11 @@ agx_status agx_pool_remove(agx_pool p, int32_t sid) {
   for (int t = sh.tile0; t < sh.tile0 + sh.ntile; t++) p->tile_scn[t] = -1;
   for (int b = sh.bnd0; b < sh.bnd0 + sh.B; b++) p->bnd_owner[b] = -1;
   for (int h = sh.halo0; h < sh.halo0 + sh.nhalo; h++) p->halo_owner[h] = -1;
-  PCK(cudaMemcpyAsync(p->tile_scn_dev, p->tile_scn.data(), p->cap_tiles * 4, cudaMemcpyHostToDevice, p->stream));
+  p->free_tiles.give(sh.tile0, sh.ntile);
+  p->free_bnd.give(sh.bnd0, sh.B);
+  p->free_halo.give(sh.halo0, sh.nhalo);
+  PCK(cudaMemcpyAsync(p->tile_scn_dev + sh.tile0, p->tile_scn.data() + sh.tile0, (size_t)sh.ntile * 4,
+                      cudaMemcpyHostToDevice, p->stream));
   p->scn_host[sid].alive = 0;
   p->scn_host[sid].active = 0;
   if ((st = push_scn(p))) return st;
@@ -2058,8 +2057,7 @@ agx_status agx_pool_remove(agx_pool p, int32_t sid) {
   bool had_ops = !sh.ops.empty();
   for (auto& op : sh.ops) if (op.idx) cudaFree((void*)op.idx);
   sh = ScnHost();
-  int ntiles = 0;
-  for (int t = 0; t < p->cap_tiles; t++) if (p->tile_scn[t] >= 0) ntiles = t + 1;
+  const int ntiles = (int)p->free_tiles.used_end();
   if (ntiles != p->d.ntiles || had_ops) {
     p->d.ntiles = ntiles;
     p->graph_valid = false;
@@ -2876,10 +2874,7 @@ agx_status agx_pool_stats_all(agx_pool p, int32_t n, const int32_t* sids, agx_st
 agx_status agx_pool_capacity(agx_pool p, int64_t* free_cells, int64_t* free_boundary, int64_t* free_halo,
                              int32_t* free_scenarios) {
   if (!p) return pfail(AGX_E_INVALID, "null pool");
-  int64_t fc = 0, run = 0, fb = 0, rb = 0, fh = 0, rh = 0;
-  for (int t = 0; t < p->cap_tiles; t++) { run = p->tile_scn[t] < 0 ? run + 1 : 0; fc = std::max(fc, run); }
-  for (int b = 0; b < p->cap_bnd; b++) { rb = p->bnd_owner[b] < 0 ? rb + 1 : 0; fb = std::max(fb, rb); }
-  for (int h = 0; h < p->cap_halo; h++) { rh = p->halo_owner[h] < 0 ? rh + 1 : 0; fh = std::max(fh, rh); }
+  const int64_t fc = p->free_tiles.largest(), fb = p->free_bnd.largest(), fh = p->free_halo.largest();
   int fs = 0;
   for (int s = 0; s < p->cap_scn; s++) fs += p->scn[s].alive ? 0 : 1;
   if (free_cells) *free_cells = fc * TILE;

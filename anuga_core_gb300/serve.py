@@ -263,6 +263,11 @@ class FloodServer:
         stream as fast as possible, every request counting as arrived."""
         pending = sorted(requests, key=lambda r: r.arrival)
         futures = {}
+        self.device_s = 0.0          # wall time spent in device chunks (launch to completion)
+        self.admit_s = 0.0           # in admissions (tables, state and boundary upload)
+        self.retire_s = 0.0          # in retirements (statistics, result read, removal)
+        self.idle_s = 0.0            # with no scenario on the device (waiting for arrivals)
+        self.chunks = 0
         t0 = time.perf_counter()
         i_next = 0
         waiting = []          # prepared, arrived, not yet admitted (in arrival order)
@@ -284,19 +289,30 @@ class FloodServer:
                     waiting.append(f.result())
                     del futures[rid]
             waiting.sort(key=lambda p: p[0].arrival)
+            ta = time.perf_counter()
             while waiting and self.fits(waiting[0][2]):
                 self._admit(waiting.pop(0), time.perf_counter() - t0)
+            self.admit_s += time.perf_counter() - ta
             if self.live:
+                tc = time.perf_counter()
                 self.pool.launch_chunk(self.chunk)
                 self.pool.wait()
+                tr = time.perf_counter()
+                self.device_s += tr - tc
+                self.chunks += 1
                 self._retire(t0)
+                self.retire_s += time.perf_counter() - tr
             else:
+                ti = time.perf_counter()
                 time.sleep(0.001)
+                self.idle_s += time.perf_counter() - ti
         wall = time.perf_counter() - t0
         lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
         return dict(requests=len(self.results), wall_s=wall, p50_s=float(np.percentile(lat, 50)),
                     p99_s=float(np.percentile(lat, 99)), cell_steps=int(self.cell_steps),
-                    cell_steps_per_s=self.cell_steps / max(wall, 1e-9))
+                    cell_steps_per_s=self.cell_steps / max(wall, 1e-9), chunks=self.chunks,
+                    device_s=self.device_s, device_cell_steps_per_s=self.cell_steps / max(self.device_s, 1e-9),
+                    admit_s=self.admit_s, retire_s=self.retire_s, idle_s=self.idle_s)
 
     def close(self):
         self.exec.shutdown(wait=False)

@@ -220,6 +220,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=60, dest="cpu_steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=256, help="serve workload: number of requests")
+    ap.add_argument("--chunk-steps", type=int, default=128, help="serve workload: device steps per chunk")
     ap.add_argument("--err-steps", type=int, default=2000, dest="err_steps",
                     help="mixed steps of the accuracy check against plain FP64 (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=500, dest="batch_steps",
@@ -645,7 +646,7 @@ def measure_serve(args, torch):
     for r in reqs:                 # build the meshes of the stream up front (mesh cache warm)
         cache.get(r.kind, r.cells)
     setup_s = time.time() - t0
-    srv = FloodServer(max_scenarios=256, chunk_steps=128, mesh_cache=cache)
+    srv = FloodServer(max_scenarios=256, chunk_steps=args.chunk_steps, mesh_cache=cache)
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
     summ = srv.run(reqs, realtime=True)
@@ -654,6 +655,9 @@ def measure_serve(args, torch):
     return {"value": summ["cell_steps_per_s"], "unit": UNIT, "requests": summ["requests"],
             "p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
             "cell_steps": summ["cell_steps"], "mesh_setup_s": setup_s,
+            "chunks": summ["chunks"], "device_s": summ["device_s"], "admit_s": summ["admit_s"],
+            "retire_s": summ["retire_s"], "idle_s": summ["idle_s"],
+            "device_cell_steps_per_s": summ["device_cell_steps_per_s"],
             "workload": "serving: %d Poisson requests (20/s, seed 99), rectangular cross or Delaunay, 10k-2M "
                         "triangles, final time 60-3600 s, DE1 mixed, continuous batching in one pool, latency = "
                         "arrival to final state on the host" % len(reqs),
@@ -668,7 +672,9 @@ def run_serve(args, torch):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 flux / f64 accumulate", "data": "synthetic",
             "config": {"workload": sv["workload"], "mesh_setup_s": sv["mesh_setup_s"]},
             "latency": {"p50_s": sv["p50_s"], "p99_s": sv["p99_s"], "wall_s": sv["wall_s"],
-                        "cell_steps": sv["cell_steps"]},
+                        "cell_steps": sv["cell_steps"], "chunks": sv["chunks"], "device_s": sv["device_s"],
+                        "admit_s": sv["admit_s"], "retire_s": sv["retire_s"], "idle_s": sv["idle_s"],
+                        "device_cell_steps_per_s": sv["device_cell_steps_per_s"]},
             "clocks": sv["clocks"]}
     print(json.dumps(line))
 
