@@ -40,11 +40,13 @@ constexpr int TPB = 256;
 #ifndef AGX_EXTRAP_ORDER
 #define AGX_EXTRAP_ORDER 1
 #endif
-// 1: the cells are sorted after every extrapolation of a step; 2: only after
-// its last (the step's stages visit the cells in one order)
+// the class bits the sort distinguishes (see k_extrap): 2 = dry cell and
+// wet/dry factor below 1
 #ifndef AGX_CLASS_BITS
 #define AGX_CLASS_BITS 2
 #endif
+// 1: the cells are sorted after every extrapolation of a step; 2: only after
+// its last (the step's stages visit the cells in one order)
 #ifndef AGX_SORT_CADENCE
 #define AGX_SORT_CADENCE 2
 #endif
